@@ -1,0 +1,568 @@
+/*
+ * branson_oracle.c — CPU restatement of Branson's replicated-mode IMC step.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker; see branson_oracle.h).  Written in
+ * plain C from the upstream algorithm; each function keeps the upstream
+ * floating-point operation order so that, built with -ffp-contract=off and
+ * the same libm, it reproduces the upstream CPU path bit for bit.  Citations
+ * are file:line within the upstream src/ directory.
+ */
+#include "branson_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* Constants namespace (constants.h:16-24) */
+static const double BO_PI = 3.1415926535897932384626433832795;
+static const double BO_C = 299.792458;  /* cm/shake */
+static const double BO_A = 0.01372;     /* GJ/cm^3/keV^4 */
+static const double BO_CUTOFF = 0.01;
+
+/* ------------------------------------------------------------------------ */
+/* Threefry2x64 with 20 rounds, restated from the published Random123
+ * specification (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as
+ * easy as 1, 2, 3", SC'11): rotation schedule for the 2x64 variant and the
+ * Threefish key-schedule parity word; key injected every four rounds with
+ * the injection index added to the last word.  Matches threefry.h:190-293
+ * (Nrounds = 20, threefry.h:178-179). */
+static inline uint64_t rotl64(uint64_t x, unsigned r) { return (x << r) | (x >> (64u - r)); }
+
+void bo_threefry2x64_20(const uint64_t ctr[2], const uint64_t key[2], uint64_t out[2]) {
+  static const unsigned R[8] = {16, 42, 12, 31, 16, 32, 24, 21};
+  const uint64_t ks[3] = {key[0], key[1], 0x1BD11BDAA9FC1A22ULL ^ key[0] ^ key[1]};
+  uint64_t x0 = ctr[0] + ks[0];
+  uint64_t x1 = ctr[1] + ks[1];
+  for (unsigned round = 0; round < 20; ++round) {
+    x0 += x1;
+    x1 = rotl64(x1, R[round & 7u]);
+    x1 ^= x0;
+    if ((round & 3u) == 3u) {
+      const unsigned s = (round >> 2) + 1u; /* injection 1..5 */
+      x0 += ks[s % 3u];
+      x1 += ks[(s + 1u) % 3u] + s;
+    }
+  }
+  out[0] = x0;
+  out[1] = x1;
+}
+
+/* _ran (RNG.h:262-285): counter {data[0], data[1] = seed<<32}, key
+ * {stream, 0}; the counter advances by one per draw; the first output word
+ * becomes u01fixedpt<double>: ((w >> 11) | 1) * 2^-53 (RNG.h:202-238). */
+double bo_rng_draw(uint32_t seed, uint64_t stream, uint64_t *counter) {
+  const uint64_t ctr[2] = {*counter, (uint64_t)seed << 32};
+  const uint64_t key[2] = {stream, 0};
+  uint64_t out[2];
+  bo_threefry2x64_20(ctr, key, out);
+  *counter += 1; /* array.h:133-141; the high word never carries in practice */
+  return (double)((out[0] >> 11) | 1u) * (1.0 / 9007199254740992.0);
+}
+
+typedef struct {
+  uint32_t seed;
+  uint64_t stream, counter;
+} bo_rng;
+
+static inline double rng_next(bo_rng *r) { return bo_rng_draw(r->seed, r->stream, &r->counter); }
+
+/* ------------------------------------------------------------------------ */
+/* geometry */
+
+void bo_cell_nodes(const bo_mesh *m, uint32_t g, double nodes[6]) {
+  const uint32_t i = g % m->ngx;
+  const uint32_t j = (g / m->ngx) % m->ngy;
+  const uint32_t k = g / (m->ngx * m->ngy);
+  nodes[0] = m->x[i];
+  nodes[1] = m->x[i + 1];
+  nodes[2] = m->y[j];
+  nodes[3] = m->y[j + 1];
+  nodes[4] = m->z[k];
+  nodes[5] = m->z[k + 1];
+}
+
+/* Cell::get_volume (cell.h:188-191) */
+static inline double cell_volume(const double n[6]) {
+  return (n[1] - n[0]) * (n[3] - n[2]) * (n[5] - n[4]);
+}
+
+/* Boundary code and neighbour of face `face` of cell g: interior faces are
+ * ELEMENT, domain faces carry the deck's boundary (proto_mesh.h:156-202). */
+static inline int cell_bc(const bo_mesh *m, uint32_t g, uint32_t face, uint32_t *next) {
+  const uint32_t i = g % m->ngx;
+  const uint32_t j = (g / m->ngx) % m->ngy;
+  const uint32_t k = g / (m->ngx * m->ngy);
+  const uint32_t sxy = m->ngx * m->ngy;
+  switch (face) {
+  case 0: if (i > 0) { *next = g - 1; return BO_ELEMENT; } break;
+  case 1: if (i + 1 < m->ngx) { *next = g + 1; return BO_ELEMENT; } break;
+  case 2: if (j > 0) { *next = g - m->ngx; return BO_ELEMENT; } break;
+  case 3: if (j + 1 < m->ngy) { *next = g + m->ngx; return BO_ELEMENT; } break;
+  case 4: if (k > 0) { *next = g - sxy; return BO_ELEMENT; } break;
+  default: if (k + 1 < m->ngz) { *next = g + sxy; return BO_ELEMENT; } break;
+  }
+  *next = g;
+  return m->bc[face];
+}
+
+/* Cell::get_source_face (cell.h:69-76): first face whose bc is SOURCE. */
+static int cell_source_face(const bo_mesh *m, uint32_t g) {
+  for (uint32_t f = 0; f < 6; ++f) {
+    uint32_t nxt;
+    if (cell_bc(m, g, f, &nxt) == BO_SOURCE)
+      return (int)f;
+  }
+  return -1;
+}
+
+/* Cell::get_face_area (cell.h:83-100) */
+static double face_area(const double n[6], int face) {
+  if (face == 0 || face == 1)
+    return (n[3] - n[2]) * (n[5] - n[4]);
+  if (face == 2 || face == 3)
+    return (n[1] - n[0]) * (n[5] - n[4]);
+  if (face == 4 || face == 5)
+    return (n[1] - n[0]) * (n[3] - n[2]);
+  return -1.0;
+}
+
+/* Cell::get_distance_to_boundary (cell.h:117-132), sgn (cell.h:23-25) */
+double bo_distance_to_boundary(const double nodes[6], const double pos[3], const double dir[3],
+                               uint32_t *surface_cross) {
+  double min_dist = 1.0e16;
+  for (uint32_t i = 0; i < 3; i++) {
+    const uint32_t index = 2 * i + (uint32_t)(0.0 < dir[i]);
+    const double dist = (nodes[index] - pos[i]) / dir[i];
+    if (dist < min_dist) {
+      min_dist = dist;
+      *surface_cross = index;
+    }
+  }
+  return min_dist;
+}
+
+/* ------------------------------------------------------------------------ */
+/* mesh physics */
+
+void bo_initialize_cells(const bo_mesh *m, bo_cells *c) {
+  const uint32_t n = m->ngx * m->ngy * m->ngz;
+  for (uint32_t g = 0; g < n; ++g) {
+    const bo_region *r = &m->regions[m->region[g]];
+    c->T_e[g] = r->T_e;
+    c->T_r[g] = r->T_r;
+    c->T_s[g] = cell_source_face(m, g) != -1 ? m->T_source : 0.0; /* mesh.h:436-437 */
+  }
+}
+
+/* Mesh::calculate_photon_energy (mesh.h:237-323) with one rank: the
+ * replicated factor is 1 and the replicated redistribution (:291-315) leaves
+ * every energy unchanged, so total_photon_E is the first pass's sum. */
+void bo_calculate_photon_energy(const bo_mesh *m, bo_cells *c, uint32_t step, double dt,
+                                bo_energy *out) {
+  const uint32_t n = m->ngx * m->ngy * m->ngz;
+  const double rf = 1.0;
+  double total = 0.0, tot_em = 0.0, tot_ce = 0.0, tot_so = 0.0, pre_mat = 0.0;
+  for (uint32_t g = 0; g < n; ++g) {
+    const bo_region *r = &m->regions[m->region[g]];
+    double nodes[6];
+    bo_cell_nodes(m, g, nodes);
+    const double vol = cell_volume(nodes);
+    const double cV = r->cv, rho = r->rho;
+    const double T = c->T_e[g], Tr = c->T_r[g], Ts = c->T_s[g];
+    const double op_a = r->opacA + r->opacB * pow(T, r->opacC); /* region.h:44-46 */
+    const double op_s = r->opacS;
+    const double f = 1.0 / (1.0 + dt * op_a * BO_C * (4.0 * BO_A * pow(T, 3) / (cV * rho)));
+    c->op_a[g] = op_a;
+    c->op_s[g] = op_s;
+    c->f[g] = f;
+    c->emission_E[g] = rf * dt * vol * f * op_a * BO_A * BO_C * pow(T, 4);
+    if (step > 1)
+      c->census_E[g] = 0.0;
+    else
+      c->census_E[g] = rf * vol * BO_A * pow(Tr, 4);
+    c->source_E[g] = rf * 0.25 * BO_A * BO_C * face_area(nodes, cell_source_face(m, g)) *
+                     pow(Ts, 4) * dt;
+    pre_mat += T * cV * vol * rho;
+    tot_em += c->emission_E[g];
+    tot_ce += c->census_E[g];
+    tot_so += c->source_E[g];
+    total += c->source_E[g] + c->census_E[g] + c->emission_E[g];
+  }
+  out->total_photon_E = total;
+  out->emission_E = tot_em;
+  out->census_E = tot_ce;
+  out->source_E = tot_so;
+  out->pre_mat_E = pre_mat;
+}
+
+/* photon count for one cell's energy (source.h:229-243): at least one. */
+static inline uint32_t photons_for(uint64_t n_user, double E, double total_E) {
+  if (!(E > 0.0))
+    return 0;
+  uint32_t t = (uint32_t)(int)((double)n_user * E / total_E);
+  return t == 0 ? 1u : t;
+}
+
+uint64_t bo_count_photons(const bo_mesh *m, const bo_cells *c, uint64_t n_user, double total_E) {
+  const uint32_t n = m->ngx * m->ngy * m->ngz;
+  uint64_t total = 0;
+  for (uint32_t g = 0; g < n; ++g)
+    total += photons_for(n_user, c->emission_E[g], total_E) +
+             photons_for(n_user, c->source_E[g], total_E);
+  return total;
+}
+
+uint64_t bo_count_initial_census(const bo_mesh *m, const bo_cells *c, uint64_t n_user,
+                                 double total_E) {
+  const uint32_t n = m->ngx * m->ngy * m->ngz;
+  uint64_t total = 0;
+  for (uint32_t g = 0; g < n; ++g)
+    total += photons_for(n_user, c->census_E[g], total_E);
+  return total;
+}
+
+/* get_uniform_position_in_cell (sampling_functions.h:22-29) */
+static void uniform_position_in_cell(const double n[6], bo_rng *r, double pos[3]) {
+  pos[0] = n[0] + rng_next(r) * (n[1] - n[0]);
+  pos[1] = n[2] + rng_next(r) * (n[3] - n[2]);
+  pos[2] = n[4] + rng_next(r) * (n[5] - n[4]);
+}
+
+/* get_uniform_position_on_face (sampling_functions.h:32-52) */
+static void uniform_position_on_face(const double n[6], bo_rng *r, int face, double pos[3]) {
+  if (face == 0 || face == 1) {
+    pos[0] = (face == 0) ? n[0] : n[1];
+    pos[1] = n[2] + rng_next(r) * (n[3] - n[2]);
+    pos[2] = n[4] + rng_next(r) * (n[5] - n[4]);
+  } else if (face == 2 || face == 3) {
+    pos[0] = n[0] + rng_next(r) * (n[1] - n[0]);
+    pos[1] = (face == 2) ? n[2] : n[3];
+    pos[2] = n[4] + rng_next(r) * (n[5] - n[4]);
+  } else {
+    pos[0] = n[0] + rng_next(r) * (n[1] - n[0]);
+    pos[1] = n[2] + rng_next(r) * (n[3] - n[2]);
+    pos[2] = (face == 4) ? n[4] : n[5];
+  }
+}
+
+/* get_uniform_angle (sampling_functions.h:57-70) */
+static void uniform_angle(bo_rng *r, double dir[3]) {
+  const double mu = rng_next(r) * 2.0 - 1.0;
+  const double phi = rng_next(r) * 2.0 * BO_PI;
+  const double sin_theta = sqrt(1.0 - mu * mu);
+  dir[0] = sin_theta * cos(phi);
+  dir[1] = sin_theta * sin(phi);
+  dir[2] = mu;
+}
+
+/* get_source_angle_on_face (sampling_functions.h:94-121); only the x faces
+ * carry the inward sign, as upstream. */
+static void source_angle_on_face(bo_rng *r, int face, double dir[3]) {
+  const double theta = acos(sqrt(rng_next(r)));
+  const double phi = rng_next(r) * 2.0 * BO_PI;
+  const double sign = (face % 2) ? -1.0 : 1.0;
+  if (face == 0 || face == 1) {
+    dir[0] = cos(theta) * sign;
+    dir[1] = sin(theta) * sin(phi);
+    dir[2] = sin(theta) * cos(phi);
+  } else if (face == 2 || face == 3) {
+    dir[0] = sin(theta) * sin(phi);
+    dir[1] = cos(theta);
+    dir[2] = sin(theta) * cos(phi);
+  } else {
+    dir[0] = sin(theta) * cos(phi);
+    dir[1] = sin(theta) * sin(phi);
+    dir[2] = cos(theta);
+  }
+}
+
+/* get_emission_photon (source.h:84-97): 7 draws */
+static void emission_photon(const bo_mesh *m, uint32_t g, double E, double dt, uint32_t seed,
+                            uint64_t stream, bo_photon *p) {
+  double n[6];
+  bo_cell_nodes(m, g, n);
+  bo_rng r = {seed, stream, 0};
+  memset(p, 0, sizeof(*p));
+  p->source_type = 2;
+  uniform_position_in_cell(n, &r, p->pos);
+  uniform_angle(&r, p->dir);
+  p->E = E; /* Photon::set_E0 sets both (photon.h:128-131) */
+  p->E0 = E;
+  p->cell = g;
+  p->life_dx = rng_next(&r) * BO_C * dt;
+  p->group = (uint32_t)floor(rng_next(&r) * (double)m->n_groups);
+  p->stream = r.stream;
+  p->counter = r.counter;
+  p->descriptor = BO_PASS;
+}
+
+/* get_boundary_source_photon (source.h:100-114): 6 draws */
+static void boundary_source_photon(const bo_mesh *m, uint32_t g, double E, double dt,
+                                   uint32_t seed, uint64_t stream, int face, bo_photon *p) {
+  double n[6];
+  bo_cell_nodes(m, g, n);
+  bo_rng r = {seed, stream, 0};
+  memset(p, 0, sizeof(*p));
+  p->source_type = 1;
+  uniform_position_on_face(n, &r, face, p->pos);
+  source_angle_on_face(&r, face, p->dir);
+  p->E = E; /* Photon::set_E0 sets both (photon.h:128-131) */
+  p->E0 = E;
+  p->cell = g;
+  p->life_dx = rng_next(&r) * BO_C * dt;
+  p->group = (uint32_t)floor(rng_next(&r) * (double)m->n_groups);
+  p->stream = r.stream;
+  p->counter = r.counter;
+  p->descriptor = BO_PASS;
+}
+
+/* get_initial_census_photon (source.h:117-131): 6 draws */
+static void initial_census_photon(const bo_mesh *m, uint32_t g, double E, double dt,
+                                  uint32_t seed, uint64_t stream, bo_photon *p) {
+  double n[6];
+  bo_cell_nodes(m, g, n);
+  bo_rng r = {seed, stream, 0};
+  memset(p, 0, sizeof(*p));
+  p->source_type = 0;
+  uniform_position_in_cell(n, &r, p->pos);
+  uniform_angle(&r, p->dir);
+  p->E = E; /* Photon::set_E0 sets both (photon.h:128-131) */
+  p->E0 = E;
+  p->cell = g;
+  p->life_dx = BO_C * dt;
+  p->group = (uint32_t)floor(rng_next(&r) * (double)m->n_groups);
+  p->stream = r.stream;
+  p->counter = r.counter;
+  p->descriptor = BO_PASS;
+}
+
+/* make_photons (source.h:294-366), rank 0: stream = 1e13*cycle + ith. */
+void bo_make_photons(const bo_mesh *m, const bo_cells *c, double dt, uint32_t cycle, uint32_t seed,
+                     uint64_t n_user, double total_E, bo_photon *out) {
+  const uint32_t n = m->ngx * m->ngy * m->ngz;
+  const uint64_t cycle_offset = 10000000000000ULL * (uint64_t)cycle;
+  uint64_t ith = 0;
+  for (uint32_t g = 0; g < n; ++g) {
+    const uint32_t n_em = photons_for(n_user, c->emission_E[g], total_E);
+    if (n_em) {
+      const double E = c->emission_E[g] / n_em;
+      for (uint32_t p = 0; p < n_em; ++p, ++ith)
+        emission_photon(m, g, E, dt, seed, cycle_offset + ith, &out[ith]);
+    }
+    const uint32_t n_so = photons_for(n_user, c->source_E[g], total_E);
+    if (n_so) {
+      const double E = c->source_E[g] / n_so;
+      const int face = cell_source_face(m, g);
+      for (uint32_t p = 0; p < n_so; ++p, ++ith)
+        boundary_source_photon(m, g, E, dt, seed, cycle_offset + ith, face, &out[ith]);
+    }
+  }
+}
+
+/* make_initial_census_photons (source.h:183-204), rank 0: stream = ith. */
+void bo_make_initial_census(const bo_mesh *m, const bo_cells *c, double dt, uint32_t seed,
+                            uint64_t n_user, double total_E, bo_photon *out) {
+  const uint32_t n = m->ngx * m->ngy * m->ngz;
+  uint64_t ith = 0;
+  for (uint32_t g = 0; g < n; ++g) {
+    const uint32_t n_ce = photons_for(n_user, c->census_E[g], total_E);
+    if (n_ce) {
+      const double E = c->census_E[g] / n_ce;
+      for (uint32_t p = 0; p < n_ce; ++p, ++ith)
+        initial_census_photon(m, g, E, dt, seed, ith, &out[ith]);
+    }
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* transport */
+
+/* sample_emission_group, Cell version (sampling_functions.h:126-138), with
+ * every group's opacity equal to op_a (Cell::set_op_a, cell.h:260-266).  A
+ * walk that runs past the last group (possible only when u rounds above the
+ * accumulated CDF) reads past the group array upstream; here it stays in
+ * the last group. */
+static uint32_t sample_emission_group(bo_rng *r, double op_a, uint32_t n_groups) {
+  double cdf_value = rng_next(r);
+  int new_group = -1;
+  const double norm_factor = 1.0 / (op_a * (double)n_groups);
+  while (cdf_value > 0) {
+    new_group++;
+    cdf_value -= op_a * norm_factor;
+    if ((uint32_t)new_group == n_groups - 1)
+      break;
+  }
+  if (new_group < 0)
+    new_group = 0;
+  return (uint32_t)new_group;
+}
+
+/* transport_photon, AoS form (history_based_transport.h:33-141). */
+static uint64_t transport_photon(const bo_mesh *m, const bo_cells *c, uint32_t seed, bo_photon *p,
+                                 double *abs_t, double *track_t) {
+  bo_rng r = {seed, p->stream, p->counter};
+  uint32_t surface_cross = 0;
+  uint32_t cell = p->cell;
+  double nodes[6];
+  bo_cell_nodes(m, cell, nodes);
+  double thread_abs = 0.0, thread_track = 0.0;
+  uint64_t segments = 0;
+  int active = 1;
+  while (active) {
+    ++segments;
+    const double sigma_s = c->op_s[cell];
+    const double sigma_a = c->op_a[cell];
+    const double f = c->f[cell];
+    const double total_sigma_s = (1.0 - f) * sigma_a + sigma_s;
+    const double dist_to_scatter =
+        (total_sigma_s > 0.0) ? -log(rng_next(&r)) / total_sigma_s : 1.0e100;
+    const double dist_to_boundary = bo_distance_to_boundary(nodes, p->pos, p->dir, &surface_cross);
+    const double dist_to_census = p->life_dx;
+    /* std::min(a, b) is (b < a) ? b : a */
+    const double db_dc = (dist_to_census < dist_to_boundary) ? dist_to_census : dist_to_boundary;
+    const double dist_to_event = (db_dc < dist_to_scatter) ? db_dc : dist_to_scatter;
+    const double absorbed_E = p->E * (1.0 - exp(-sigma_a * f * dist_to_event));
+    thread_abs += absorbed_E;
+    thread_track += absorbed_E / (sigma_a * f);
+    p->E = p->E - absorbed_E;
+    p->pos[0] += p->dir[0] * dist_to_event; /* Photon::move (photon.h:109-114) */
+    p->pos[1] += p->dir[1] * dist_to_event;
+    p->pos[2] += p->dir[2] * dist_to_event;
+    p->life_dx -= dist_to_event;
+    if (p->E / p->E0 < BO_CUTOFF) { /* below_cutoff (photon.h:47-49) */
+      thread_abs += p->E;
+      abs_t[cell] += thread_abs;
+      track_t[cell] += thread_track;
+      active = 0;
+      p->descriptor = BO_KILLED;
+    } else if (dist_to_event == dist_to_scatter) {
+      uniform_angle(&r, p->dir);
+      if (rng_next(&r) > (sigma_s / ((1.0 - f) * sigma_a + sigma_s)))
+        p->group = sample_emission_group(&r, sigma_a, m->n_groups);
+      p->descriptor = BO_SCATTER;
+    } else if (dist_to_event == dist_to_boundary) {
+      uint32_t next;
+      const int bc = cell_bc(m, cell, surface_cross, &next);
+      if (bc == BO_ELEMENT) {
+        abs_t[cell] += thread_abs;
+        track_t[cell] += thread_track;
+        p->cell = next;
+        cell = next;
+        bo_cell_nodes(m, cell, nodes);
+        p->descriptor = BO_BOUND;
+        thread_abs = 0.0;
+        thread_track = 0.0;
+      } else if (bc == BO_PROCESSOR) {
+        active = 0;
+        p->cell = next;
+        p->descriptor = BO_PASS;
+        abs_t[cell] += thread_abs;
+        track_t[cell] += thread_track;
+      } else if (bc == BO_VACUUM || bc == BO_SOURCE) {
+        active = 0;
+        p->descriptor = BO_EXIT;
+        abs_t[cell] += thread_abs;
+        track_t[cell] += thread_track;
+      } else { /* REFLECT: Photon::reflect (photon.h:151-155) */
+        p->dir[surface_cross / 2] = -p->dir[surface_cross / 2];
+        p->descriptor = BO_BOUND;
+      }
+    } else if (dist_to_event == dist_to_census) {
+      active = 0;
+      p->descriptor = BO_CENSUS;
+      abs_t[cell] += thread_abs;
+      track_t[cell] += thread_track;
+    }
+  }
+  p->counter = r.counter;
+  return segments;
+}
+
+/* history_cpu_transport_photons (history_based_transport.h:279-308):
+ * OpenMP guided loop, one tally array per thread, merged cell by cell in
+ * thread order. */
+uint64_t bo_transport(const bo_mesh *m, const bo_cells *c, uint32_t seed, bo_photon *photons,
+                      size_t n, double *abs_E, double *track_E, int n_threads) {
+  const size_t n_cells = (size_t)m->ngx * m->ngy * m->ngz;
+  int nt = 1;
+#ifdef _OPENMP
+  nt = n_threads > 0 ? n_threads : omp_get_max_threads();
+#else
+  (void)n_threads;
+#endif
+  double *tallies = (double *)calloc((size_t)nt * n_cells * 2, sizeof(double));
+  uint64_t segments = 0;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nt) reduction(+ : segments)
+#endif
+  {
+    int t = 0;
+#ifdef _OPENMP
+    t = omp_get_thread_num();
+#endif
+    double *ta = tallies + (size_t)t * n_cells * 2;
+    double *tt = ta + n_cells;
+#ifdef _OPENMP
+#pragma omp for schedule(guided)
+#endif
+    for (long i = 0; i < (long)n; ++i)
+      segments += transport_photon(m, c, seed, &photons[i], ta, tt);
+  }
+  for (size_t g = 0; g < n_cells; ++g) {
+    double a = 0.0, tr = 0.0; /* Cell_Tally starts at zero (cell_tally.h:32-34) */
+    for (int t = 0; t < nt; ++t) {
+      a += tallies[(size_t)t * n_cells * 2 + g];
+      tr += tallies[(size_t)t * n_cells * 2 + n_cells + g];
+    }
+    abs_E[g] = a;
+    track_E[g] = tr;
+  }
+  free(tallies);
+  return segments;
+}
+
+/* post_process_photons, AoS (post_process_functions.h:33-59) */
+size_t bo_post_process(double next_dt, bo_photon *photons, size_t n, bo_photon *census_out,
+                       double *census_E, double *exit_E) {
+  size_t nc = 0;
+  for (size_t i = 0; i < n; ++i) {
+    bo_photon *p = &photons[i];
+    if (p->descriptor == BO_EXIT) {
+      *exit_E += p->E;
+    } else if (p->descriptor == BO_CENSUS) {
+      p->life_dx = BO_C * next_dt;
+      if (census_out)
+        census_out[nc] = *p;
+      ++nc;
+      *census_E += p->E;
+    }
+  }
+  return nc;
+}
+
+/* Mesh::update_temperature (mesh.h:349-362, :419-422) */
+void bo_update_temperature(const bo_mesh *m, bo_cells *c, double dt, double *abs_E,
+                           double *track_E, double *total_abs_E, double *post_mat_E) {
+  const uint32_t n = m->ngx * m->ngy * m->ngz;
+  double tot_abs = 0.0, tot_mat = 0.0;
+  for (uint32_t g = 0; g < n; ++g) {
+    const bo_region *r = &m->regions[m->region[g]];
+    const double cV = r->cv, rho = r->rho;
+    double nodes[6];
+    bo_cell_nodes(m, g, nodes);
+    const double vol = cell_volume(nodes);
+    const double T = c->T_e[g];
+    const double T_new = T + (abs_E[g] - c->emission_E[g]) / (cV * vol * rho);
+    c->T_r_diag[g] = pow(track_E[g] / (vol * dt * BO_A * BO_C), 0.25);
+    c->T_e[g] = T_new;
+    tot_abs += abs_E[g];
+    tot_mat += T_new * cV * vol * rho;
+    abs_E[g] = 0.0;
+    track_E[g] = 0.0;
+  }
+  *total_abs_E = tot_abs;
+  *post_mat_E = tot_mat;
+}
