@@ -1,0 +1,353 @@
+"""Benchmark: histories/s of the replicated IMC step on one GB300.
+
+Workload (default): the 50^3 gray hot zone (0.02 cm cells, central 10^3 hot
+block at 1 keV in a 0.05 keV surround, sigma_a = 10 T^-3, rho = 1, cV = 0.1,
+vacuum boundaries, dt = 0.01 sh) with 1e7 photons per step, seed 777,
+synthetic deck generated in-process (no public dataset exists for this
+metric).  A step is one full replicated time step on the device: per-cell
+energies, sourcing, history transport, census compaction, tally reduce and
+temperature update.  The photon bank (~1 GB per step) is far larger than L2,
+so no flush is needed between steps.
+
+value     histories transported / device time of K steps (CUDA events on the
+          stream the kernels run on), max over ranks
+e2e       the same metric through the drop-in call bgs_replicated_transport
+          on pinned host buffers, copies in the timed region
+roofline  k_transport_history: algorithmic bytes per launch / its CUDA-event
+          duration against the measured HBM copy bandwidth
+cpu_baseline  the oracle (C restatement, OpenMP on every host core) on a
+          bounded sample of the same deck, histories / transport time
+
+--impl reference runs the CPU implementation (the oracle port of the
+upstream history loop, all host threads) on the same workload and metric.
+Multi-GPU (torchrun): independent replicas, one per GPU (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "histories/s on 1 GB300 (plain vs batched); adjoint/forward time at 1% tally err"
+UNIT = "histories/s"
+# algorithmic bytes of k_transport_history per launch: each history's state
+# read once and written once (96 B each way: pos 24, dir 24, E 8, E0 8,
+# life 8, cell 4, group 4, counter 8, stream 8) plus per cell 72 B of
+# coefficients/geometry read and 32 B of tallies written
+BYTES_PER_HISTORY = 192
+BYTES_PER_CELL = 104
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--workload", default="hot_zone", choices=["hot_zone", "marshak", "hohlraum"])
+    p.add_argument("--photons", type=float, default=None)
+    p.add_argument("--side", type=int, default=None)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--cpu-photons", type=float, default=1e6)
+    return p.parse_args()
+
+
+def make_deck(args):
+    from branson_gb300 import deck as D
+    steps = 10 ** 6  # keep stepping past the deck's own end time
+    if args.workload == "hot_zone":
+        side = args.side or 50
+        photons = int(args.photons or 1e7)
+        dk = D.hot_zone(n_per_axis=side, photons=photons, n_steps=10)
+        cfg = {"workload": f"hot_zone_{side}^3", "cells": side ** 3, "photons_per_step": photons,
+               "dt": 0.01, "groups": 1}
+    elif args.workload == "marshak":
+        photons = int(args.photons or 1e6)
+        dk = D.marshak_wave(n_cells=args.side or 100, photons=photons, n_steps=50)
+        cfg = {"workload": f"marshak_{args.side or 100}x1x1", "cells": args.side or 100,
+               "photons_per_step": photons, "dt": 0.001, "groups": 1}
+    else:
+        side = args.side or 60
+        photons = int(args.photons or 5e7)
+        dk = D.hohlraum(n_per_axis=side, photons=photons, n_steps=5, n_groups=30)
+        cfg = {"workload": f"hohlraum_{side}^3_30g", "cells": side ** 3, "photons_per_step": photons,
+               "dt": 0.005, "groups": 30}
+    dk.t_stop = dk.dt_start * steps
+    cfg.update({"seed": dk.seed, "l2": "bank > L2 (no flush needed)", "data": "synthetic deck"})
+    return dk, cfg
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi sampler for the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{index}.csv")
+
+    def start(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        with open(self.path) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower() in ("active", "1"):
+                        reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_port_rate(dk_gpu, photons: float, threads: int, steps: int = 1):
+    """Oracle (C port of the upstream history loop) on the host cores."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import copy
+    import oracle as O
+    dk = copy.deepcopy(dk_gpu)
+    dk.photons = int(photons)
+    orc = O.Oracle(dk, n_threads=threads)
+    hist = 0
+    secs = 0.0
+    segs = 0
+    for _ in range(steps):
+        r = orc.step()
+        hist += len(r.source)
+        secs += r.transport_s
+        segs += r.segments
+    return hist, secs, segs
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    dk, cfg = make_deck(args)
+    threads = os.cpu_count() or 1
+    photons = args.cpu_photons
+    cfg = dict(cfg, photons_per_step=int(photons), sample="photons per step reduced to fit minutes")
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import copy
+    import oracle as O
+    d2 = copy.deepcopy(dk)
+    d2.photons = int(photons)
+    orc = O.Oracle(d2, n_threads=threads)
+    for _ in range(args.warmup):
+        orc.step()
+    hist, secs = 0, 0.0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r = orc.step()
+        hist += len(r.source)
+        secs += r.transport_s
+    wall = time.perf_counter() - t0
+    v = hist / secs
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": cfg, "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} steps of the deck at {int(photons)} photons/step; "
+                                       f"transport time only (replicated_transport timer)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": wall}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local):
+    import numpy as np
+    import torch
+
+    dev = local if world > 1 else 0
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from branson_gb300 import _lib
+    from branson_gb300.engine import ReplicatedIMC, records_to_arrays
+
+    dk, cfg = make_deck(args)
+    dk.seed = (dk.seed + 7919 * rank) & 0xFFFFFFFF  # independent replica per rank
+    stream = torch.cuda.Stream(device=dev)
+    imc = ReplicatedIMC(dk, device=dev, stream=stream.cuda_stream)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        imc.step(sync=True)
+    barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(dev)
+    clocks.start()
+    launches0 = imc.kernel_launches()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    hist = 0
+    segs = 0
+    transport_ms = []
+    ev0.record(stream)
+    for _ in range(args.steps):
+        r = imc.step(sync=True)
+        hist += r.n_transported
+        segs += r.n_segments
+        ms, _k = imc.last_transport_ms()
+        transport_ms.append((ms, r.n_transported))
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    elapsed = ev0.elapsed_time(ev1) / 1e3
+    launches = imc.kernel_launches() - launches0
+    clk = clocks.stop()
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([elapsed], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+        h = torch.tensor([float(hist)], device=f"cuda:{dev}")
+        dist.all_reduce(h)
+        hist_all = float(h.item())
+    else:
+        hist_all = float(hist)
+    value = hist_all / elapsed
+
+    # roofline of the dominant kernel (k_transport_history), live CUDA events
+    k_ms = sum(m for m, _ in transport_ms) / len(transport_ms)
+    k_hist = sum(n for _, n in transport_ms) / len(transport_ms)
+    alg_bytes = BYTES_PER_HISTORY * k_hist + BYTES_PER_CELL * dk.n_cells
+    achieved = alg_bytes / (k_ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peak_hbm()
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "transport_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as fh:
+            t = json.load(fh)
+        traffic = t.get("bytes_per_history", 0) * k_hist + t.get("bytes_per_cell", 0) * dk.n_cells
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs",
+                "kernel": "k_transport_history", "kernel_ms": k_ms,
+                "segments_per_s": segs / (sum(m for m, _ in transport_ms) * 1e-3),
+                "note": "FP64-issue bound: the HBM fraction is small by construction"}
+
+    # end to end through the drop-in call on pinned host buffers
+    e2e = None
+    if not args.no_e2e and rank == 0:
+        e2e = e2e_dropin(imc, dk, args)
+
+    cpu = None
+    if not args.no_cpu_baseline and rank == 0 and world == 1:
+        threads = os.cpu_count() or 1
+        h, s, sg = cpu_port_rate(dk, args.cpu_photons, threads)
+        cpu = {"value": h / s, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"1 step of the same deck at {int(args.cpu_photons)} photons ({h} histories), "
+                         f"transport time"}
+    imc.close()
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": dict(cfg, parallelism=f"replicas{world}"), "roofline": roofline,
+                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
+                "segments_per_s": segs / elapsed * world, "histories_per_step": hist / args.steps}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def e2e_dropin(imc, dk, args):
+    """Drop-in replicated_transport on pinned host buffers, copies timed."""
+    import numpy as np
+    from branson_gb300._lib import PhotonArrays
+    # inputs: the current step's photon list, made on the device and copied out
+    step, dt = imc.step_no, imc.dt
+    imc.calculate_photon_energy(step, dt)
+    imc.source(step, dt)
+    n = imc.bank_size()
+    src = imc.photons(0, n)
+    work = PhotonArrays(n, pinned=True)
+    census = PhotonArrays(n, pinned=True)
+    nd = imc.next_dt() if imc.next_dt() > 0 else dt
+    hist, secs = 0, 0.0
+    k = max(1, min(args.steps, 3))
+    for it in range(k + 1):
+        for name in work.arrays:
+            np.copyto(work[name], src[name])
+        t0 = time.perf_counter()
+        abs_E, trk_E, cen, ce, ex = imc.replicated_transport(work, nd, census=census)
+        t1 = time.perf_counter()
+        if it > 0:  # first call is warm-up
+            hist += n
+            secs += t1 - t0
+    in_bytes = sum(a.nbytes for a in src.arrays.values())
+    out_bytes = n * (6 * 8 + 8 + 8 + 4 + 4 + 1 + 8) + cen.n * sum(a.itemsize for a in src.arrays.values()) \
+        + 2 * 8 * dk.n_cells
+    return {"value": hist / secs, "unit": UNIT, "h2d_bytes_per_step": int(in_bytes),
+            "d2h_bytes_per_step": int(out_bytes), "call": "bgs_replicated_transport", "steps": k}
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,615 @@
+// C ABI of the GB300 replicated IMC step (include/branson_gb300.h): context
+// lifetime, device memory, the staged step and the host-buffer drop-in for
+// replicated_transport.  Host-side orchestration only; all arithmetic runs
+// in the kernels of bgs_mesh.cu, bgs_source.cu and bgs_transport.cu.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/branson_gb300.h"
+#include "bgs_kernels.cuh"
+
+using namespace bgs;
+
+struct bgs_context {
+  int device = 0;
+  int n_sm = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  uint32_t seed = 0;
+  unsigned long long n_user = 0;
+  unsigned long long capacity = 0;
+  bool has_mesh = false;
+  bool xs_dirty = true;
+
+  MeshDev mesh{};
+  CellsDev cells{};
+  std::vector<void *> mesh_allocs;  // freed on set_mesh / destroy
+  double *d_mat_E = nullptr, *d_abs = nullptr, *d_track = nullptr, *d_mat_part = nullptr;
+  double *d_energy_part = nullptr;
+  unsigned long long *d_tile_cells = nullptr;
+
+  Bank bank[2]{};
+  int cur = 0;
+  std::vector<void *> bank_allocs;
+  unsigned long long *d_off_bank = nullptr, *d_tile_bank = nullptr, *d_maxbits = nullptr;
+
+  DeviceDiag *d_diag = nullptr;
+  DeviceDiag *h_diag = nullptr;  // pinned
+  TransportLaunch tshape{};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  uint32_t last_launches = 0;
+  unsigned long long launches = 0;
+  bool bank_is_census = true;  // current bank holds a census (after transport)
+  std::string err;
+};
+
+namespace {
+
+int fail(bgs_context *ctx, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (ctx) ctx->err = buf;
+  return code;
+}
+
+#define BGS_CUDA(ctx, call)                                                                   \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess)                                                                    \
+      return fail((ctx), BGS_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));       \
+  } while (0)
+
+#define BGS_LAUNCHED(ctx, n)                                                                  \
+  do {                                                                                        \
+    cudaError_t e_ = cudaGetLastError();                                                      \
+    if (e_ != cudaSuccess)                                                                    \
+      return fail((ctx), BGS_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e_));   \
+    (ctx)->launches += (n);                                                                   \
+  } while (0)
+
+template <typename T>
+int dev_alloc(bgs_context *ctx, std::vector<void *> &list, T **p, size_t count) {
+  void *q = nullptr;
+  const size_t bytes = count * sizeof(T) > 0 ? count * sizeof(T) : 16;
+  cudaError_t e = cudaMalloc(&q, bytes);
+  if (e != cudaSuccess)
+    return fail(ctx, BGS_ERR_CUDA, "cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+  list.push_back(q);
+  *p = static_cast<T *>(q);
+  return BGS_OK;
+}
+
+void free_list(std::vector<void *> &list) {
+  for (void *p : list) cudaFree(p);
+  list.clear();
+}
+
+int set_device(bgs_context *ctx) {
+  BGS_CUDA(ctx, cudaSetDevice(ctx->device));
+  return BGS_OK;
+}
+
+int check_flags(bgs_context *ctx, uint32_t flags) {
+  if (!flags) return BGS_OK;
+  std::string what;
+  if (flags & FLAG_CAPACITY) what += " photon-bank capacity exceeded (no photons made);";
+  if (flags & FLAG_TALLY_RANGE) what += " tally contribution outside the fixed-point range;";
+  if (flags & FLAG_SEGMENT_LIMIT) what += " a history hit the segment limit;";
+  if (flags & FLAG_BAD_CELL) what += " a photon referenced a cell outside the mesh;";
+  if (flags & FLAG_NAN) what += " a non-finite tally contribution was dropped;";
+  return fail(ctx, (flags & FLAG_CAPACITY) ? BGS_ERR_CAPACITY : BGS_ERR_DEVICE,
+              "device check fired (flags 0x%x):%s", flags, what.c_str());
+}
+
+int read_diag(bgs_context *ctx) {
+  BGS_CUDA(ctx, cudaMemcpyAsync(ctx->h_diag, ctx->d_diag, sizeof(DeviceDiag), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+  BGS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return BGS_OK;
+}
+
+void fill_transport_diag(const DeviceDiag &d, bgs_transport_diag *out) {
+  out->n_transported = d.n_bank;
+  out->n_census = d.n_census_out;
+  out->n_segments = d.n_segments;
+  out->census_E = d.census_E;
+  out->exit_E = d.exit_E;
+  out->absorbed_E = d.absorbed_E;
+  out->post_mat_E = d.post_mat_E;
+  out->device_flags = d.flags;
+  out->reserved = 0;
+}
+
+double *field_ptr(bgs_context *ctx, int field) {
+  CellsDev &c = ctx->cells;
+  switch (field) {
+    case BGS_FIELD_T_E: return c.T_e;
+    case BGS_FIELD_T_R: return c.T_r_diag;
+    case BGS_FIELD_OP_A: return c.op_a;
+    case BGS_FIELD_OP_S: return c.op_s;
+    case BGS_FIELD_F: return c.f;
+    case BGS_FIELD_EMISSION_E: return c.em_E;
+    case BGS_FIELD_CENSUS_E: return c.ce_E;
+    case BGS_FIELD_SOURCE_E: return c.so_E;
+    case BGS_FIELD_ABS_E: return ctx->d_abs;
+    case BGS_FIELD_TRACK_E: return ctx->d_track;
+    default: return nullptr;
+  }
+}
+
+int alloc_bank(bgs_context *ctx, Bank &b, unsigned long long cap) {
+  int rc;
+  if ((rc = dev_alloc(ctx, ctx->bank_allocs, &b.px, cap))) return rc;
+  if ((rc = dev_alloc(ctx, ctx->bank_allocs, &b.py, cap))) return rc;
+  if ((rc = dev_alloc(ctx, ctx->bank_allocs, &b.pz, cap))) return rc;
+  if ((rc = dev_alloc(ctx, ctx->bank_allocs, &b.dx, cap))) return rc;
+  if ((rc = dev_alloc(ctx, ctx->bank_allocs, &b.dy, cap))) return rc;
+  if ((rc = dev_alloc(ctx, ctx->bank_allocs, &b.dz, cap))) return rc;
+  if ((rc = dev_alloc(ctx, ctx->bank_allocs, &b.E, cap))) return rc;
+  if ((rc = dev_alloc(ctx, ctx->bank_allocs, &b.E0, cap))) return rc;
+  if ((rc = dev_alloc(ctx, ctx->bank_allocs, &b.life, cap))) return rc;
+  if ((rc = dev_alloc(ctx, ctx->bank_allocs, &b.cell, cap))) return rc;
+  if ((rc = dev_alloc(ctx, ctx->bank_allocs, &b.group, cap))) return rc;
+  if ((rc = dev_alloc(ctx, ctx->bank_allocs, &b.desc, cap))) return rc;
+  if ((rc = dev_alloc(ctx, ctx->bank_allocs, &b.stype, cap))) return rc;
+  if ((rc = dev_alloc(ctx, ctx->bank_allocs, &b.stream, cap))) return rc;
+  if ((rc = dev_alloc(ctx, ctx->bank_allocs, &b.ctr, cap))) return rc;
+  return BGS_OK;
+}
+
+// copy count photons between a bank (at offset) and host SoA arrays
+int copy_photons(bgs_context *ctx, const Bank &b, unsigned long long offset, unsigned long long n,
+                 const bgs_photons_host *h, bool to_host) {
+  if (n == 0) return BGS_OK;
+  const cudaMemcpyKind kind = to_host ? cudaMemcpyDeviceToHost : cudaMemcpyHostToDevice;
+#define BGS_CP(dev, host, T)                                                                    \
+  if (h->host) {                                                                                \
+    if (to_host)                                                                                \
+      BGS_CUDA(ctx, cudaMemcpyAsync(h->host, b.dev + offset, n * sizeof(T), kind, ctx->stream)); \
+    else                                                                                        \
+      BGS_CUDA(ctx, cudaMemcpyAsync(b.dev + offset, h->host, n * sizeof(T), kind, ctx->stream)); \
+  }
+  BGS_CP(px, pos_x, double)
+  BGS_CP(py, pos_y, double)
+  BGS_CP(pz, pos_z, double)
+  BGS_CP(dx, dir_x, double)
+  BGS_CP(dy, dir_y, double)
+  BGS_CP(dz, dir_z, double)
+  BGS_CP(E, E, double)
+  BGS_CP(E0, E0, double)
+  BGS_CP(life, life_dx, double)
+  BGS_CP(cell, cell, uint32_t)
+  BGS_CP(group, group, uint32_t)
+  BGS_CP(desc, descriptor, uint8_t)
+  BGS_CP(stype, source_type, uint8_t)
+  BGS_CP(stream, rng_stream, uint64_t)
+  BGS_CP(ctr, rng_counter, uint64_t)
+#undef BGS_CP
+  return BGS_OK;
+}
+
+__global__ void k_set_bank_size(DeviceDiag *d, unsigned long long n) {
+  d->n_bank = n;
+  d->n_census_in = n;
+  d->census_E_in = 0.0;
+  d->n_new = 0;
+  d->n_init_census = 0;
+}
+
+__global__ void k_reset_queue(DeviceDiag *d) {
+  d->work_counter = 0;
+  d->n_segments = 0;
+}
+
+}  // namespace
+
+// ===================================================================== C ABI
+extern "C" {
+
+const char *bgs_version(void) { return "branson_gb300 0.1 (sm_103a)"; }
+
+const char *bgs_status_string(int status) {
+  switch (status) {
+    case BGS_OK: return "ok";
+    case BGS_ERR_INVALID: return "invalid argument";
+    case BGS_ERR_CUDA: return "CUDA runtime error";
+    case BGS_ERR_CAPACITY: return "capacity exceeded";
+    case BGS_ERR_STATE: return "call out of order";
+    case BGS_ERR_DEVICE: return "device-side check fired";
+    case BGS_ERR_NO_DEVICE: return "no usable sm_103 device";
+    default: return "unknown status";
+  }
+}
+
+const char *bgs_last_error(const bgs_context *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int bgs_create(bgs_context **out, int device, uint64_t photon_capacity, void *stream, uint32_t seed,
+               uint64_t n_user_photons) {
+  if (!out) return BGS_ERR_INVALID;
+  *out = nullptr;
+  int n_dev = 0;
+  if (cudaGetDeviceCount(&n_dev) != cudaSuccess || n_dev <= device || device < 0)
+    return BGS_ERR_NO_DEVICE;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return BGS_ERR_NO_DEVICE;
+  if (prop.major != 10 || prop.minor != 3) return BGS_ERR_NO_DEVICE;  // built for sm_103a only
+  bgs_context *ctx = new (std::nothrow) bgs_context();
+  if (!ctx) return BGS_ERR_INVALID;
+  ctx->device = device;
+  ctx->n_sm = prop.multiProcessorCount;
+  ctx->seed = seed;
+  ctx->n_user = n_user_photons;
+  ctx->capacity = photon_capacity > 0 ? photon_capacity : 1;
+  int rc = set_device(ctx);
+  if (!rc && stream) {
+    ctx->stream = static_cast<cudaStream_t>(stream);
+  } else if (!rc) {
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) rc = BGS_ERR_CUDA;
+    ctx->own_stream = true;
+  }
+  if (!rc && (cudaMalloc(&ctx->d_diag, sizeof(DeviceDiag)) != cudaSuccess ||
+              cudaMallocHost(&ctx->h_diag, sizeof(DeviceDiag)) != cudaSuccess ||
+              cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess))
+    rc = BGS_ERR_CUDA;
+  if (!rc) rc = alloc_bank(ctx, ctx->bank[0], ctx->capacity);
+  if (!rc) rc = alloc_bank(ctx, ctx->bank[1], ctx->capacity);
+  if (!rc) {
+    const uint32_t tiles = scan_tiles_needed(ctx->capacity) + 1;
+    rc = dev_alloc(ctx, ctx->bank_allocs, &ctx->d_off_bank, ctx->capacity + 1);
+    if (!rc) rc = dev_alloc(ctx, ctx->bank_allocs, &ctx->d_tile_bank, (size_t)tiles + 1);
+    if (!rc) rc = dev_alloc(ctx, ctx->bank_allocs, &ctx->d_maxbits, 2);
+  }
+  if (!rc && cudaMemsetAsync(ctx->d_diag, 0, sizeof(DeviceDiag), ctx->stream) != cudaSuccess) rc = BGS_ERR_CUDA;
+  if (!rc) ctx->tshape = transport_launch_shape(ctx->n_sm);
+  if (rc) {
+    bgs_destroy(ctx);
+    return rc;
+  }
+  *out = ctx;
+  return BGS_OK;
+}
+
+int bgs_destroy(bgs_context *ctx) {
+  if (!ctx) return BGS_OK;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  free_list(ctx->mesh_allocs);
+  free_list(ctx->bank_allocs);
+  if (ctx->d_diag) cudaFree(ctx->d_diag);
+  if (ctx->h_diag) cudaFreeHost(ctx->h_diag);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return BGS_OK;
+}
+
+uint32_t bgs_n_cells(const bgs_context *ctx) { return ctx && ctx->has_mesh ? ctx->mesh.n_cells : 0u; }
+
+uint64_t bgs_kernel_launch_count(const bgs_context *ctx) { return ctx ? ctx->launches : 0ULL; }
+
+int bgs_set_mesh(bgs_context *ctx, const bgs_mesh_desc *md) {
+  if (!ctx || !md) return BGS_ERR_INVALID;
+  if (!md->x_planes || !md->y_planes || !md->z_planes || !md->cell_region || !md->regions)
+    return fail(ctx, BGS_ERR_INVALID, "mesh description has a null array");
+  const uint64_t n64 = (uint64_t)md->ngx * md->ngy * md->ngz;
+  if (md->ngx == 0 || md->ngy == 0 || md->ngz == 0 || n64 > 0x7fffffffULL)
+    return fail(ctx, BGS_ERR_INVALID, "mesh dimensions %u x %u x %u out of range", md->ngx, md->ngy,
+                md->ngz);
+  if (md->n_regions == 0 || md->n_groups == 0)
+    return fail(ctx, BGS_ERR_INVALID, "need at least one region and one group");
+  const uint32_t n = (uint32_t)n64;
+  for (uint32_t g = 0; g < n; ++g)
+    if (md->cell_region[g] >= md->n_regions)
+      return fail(ctx, BGS_ERR_INVALID, "cell %u names region %u of %u", g, md->cell_region[g],
+                  md->n_regions);
+  for (int f = 0; f < 6; ++f)
+    if (md->bc[f] != BGS_REFLECT && md->bc[f] != BGS_VACUUM && md->bc[f] != BGS_SOURCE)
+      return fail(ctx, BGS_ERR_INVALID, "boundary %d has code %d (REFLECT, VACUUM or SOURCE)", f,
+                  md->bc[f]);
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  BGS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  free_list(ctx->mesh_allocs);
+  ctx->has_mesh = false;
+  double *x, *y, *z, *regions;
+  uint32_t *region;
+  auto &L = ctx->mesh_allocs;
+  if ((rc = dev_alloc(ctx, L, &x, md->ngx + 1)) || (rc = dev_alloc(ctx, L, &y, md->ngy + 1)) ||
+      (rc = dev_alloc(ctx, L, &z, md->ngz + 1)) || (rc = dev_alloc(ctx, L, &region, n)) ||
+      (rc = dev_alloc(ctx, L, &regions, (size_t)md->n_regions * 8)))
+    return rc;
+  CellsDev &c = ctx->cells;
+  double **dbl[] = {&c.T_e, &c.T_r, &c.T_s, &c.op_a, &c.op_s, &c.f, &c.em_E, &c.ce_E, &c.so_E,
+                    &c.T_r_diag, &c.group_v, &ctx->d_mat_E, &ctx->d_abs, &ctx->d_track};
+  for (double **p : dbl)
+    if ((rc = dev_alloc(ctx, L, p, n))) return rc;
+  if ((rc = dev_alloc(ctx, L, &c.xs, n)) || (rc = dev_alloc(ctx, L, &c.tally, n)) ||
+      (rc = dev_alloc(ctx, L, &c.source_face, n)) || (rc = dev_alloc(ctx, L, &c.n_em, n)) ||
+      (rc = dev_alloc(ctx, L, &c.n_so, n)) || (rc = dev_alloc(ctx, L, &c.n_ce, n)) ||
+      (rc = dev_alloc(ctx, L, &c.off_new, (size_t)n + 1)) ||
+      (rc = dev_alloc(ctx, L, &c.off_ce, (size_t)n + 1)) ||
+      (rc = dev_alloc(ctx, L, &ctx->d_mat_part, update_temperature_parts(n) + 1)) ||
+      (rc = dev_alloc(ctx, L, &ctx->d_energy_part, 5 * (size_t)energy_parts(n) + 5)) ||
+      (rc = dev_alloc(ctx, L, &ctx->d_tile_cells, (size_t)scan_tiles_needed(n) + 2)))
+    return rc;
+  BGS_CUDA(ctx, cudaMemcpyAsync(x, md->x_planes, (md->ngx + 1) * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  BGS_CUDA(ctx, cudaMemcpyAsync(y, md->y_planes, (md->ngy + 1) * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  BGS_CUDA(ctx, cudaMemcpyAsync(z, md->z_planes, (md->ngz + 1) * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  BGS_CUDA(ctx, cudaMemcpyAsync(region, md->cell_region, n * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream));
+  BGS_CUDA(ctx, cudaMemcpyAsync(regions, md->regions, (size_t)md->n_regions * 8 * sizeof(double),
+                                cudaMemcpyHostToDevice, ctx->stream));
+  BGS_CUDA(ctx, cudaMemsetAsync(c.tally, 0, n * sizeof(TallyCell), ctx->stream));
+  BGS_CUDA(ctx, cudaMemsetAsync(c.op_a, 0, n * sizeof(double), ctx->stream));
+  BGS_CUDA(ctx, cudaMemsetAsync(c.op_s, 0, n * sizeof(double), ctx->stream));
+  BGS_CUDA(ctx, cudaMemsetAsync(c.f, 0, n * sizeof(double), ctx->stream));
+  MeshDev &m = ctx->mesh;
+  m.ngx = md->ngx; m.ngy = md->ngy; m.ngz = md->ngz; m.n_groups = md->n_groups;
+  m.n_cells = n; m.n_regions = md->n_regions;
+  m.x = x; m.y = y; m.z = z; m.region = region; m.regions = regions;
+  for (int f = 0; f < 6; ++f) m.bc[f] = md->bc[f];
+  m.T_source = md->T_source;
+  launch_init_cells(m, c, ctx->stream);
+  BGS_LAUNCHED(ctx, 1);
+  BGS_CUDA(ctx, cudaMemsetAsync(ctx->d_diag, 0, sizeof(DeviceDiag), ctx->stream));
+  BGS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->has_mesh = true;
+  ctx->xs_dirty = true;
+  ctx->bank_is_census = true;
+  return BGS_OK;
+}
+
+int bgs_get_cell_field(bgs_context *ctx, int field, double *host_out) {
+  if (!ctx || !host_out) return BGS_ERR_INVALID;
+  if (!ctx->has_mesh) return fail(ctx, BGS_ERR_STATE, "no mesh");
+  double *p = field_ptr(ctx, field);
+  if (!p) return fail(ctx, BGS_ERR_INVALID, "unknown cell field %d", field);
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  BGS_CUDA(ctx, cudaMemcpyAsync(host_out, p, ctx->mesh.n_cells * sizeof(double), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+  BGS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return BGS_OK;
+}
+
+int bgs_set_cell_field(bgs_context *ctx, int field, const double *host_in) {
+  if (!ctx || !host_in) return BGS_ERR_INVALID;
+  if (!ctx->has_mesh) return fail(ctx, BGS_ERR_STATE, "no mesh");
+  if (field != BGS_FIELD_T_E && field != BGS_FIELD_OP_A && field != BGS_FIELD_OP_S && field != BGS_FIELD_F)
+    return fail(ctx, BGS_ERR_INVALID, "cell field %d is not writable", field);
+  double *p = field_ptr(ctx, field);
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  BGS_CUDA(ctx, cudaMemcpyAsync(p, host_in, ctx->mesh.n_cells * sizeof(double), cudaMemcpyHostToDevice,
+                                ctx->stream));
+  BGS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (field != BGS_FIELD_T_E) ctx->xs_dirty = true;
+  return BGS_OK;
+}
+
+int bgs_calculate_photon_energy(bgs_context *ctx, uint32_t step, double dt, bgs_energy_diag *out) {
+  if (!ctx) return BGS_ERR_INVALID;
+  if (!ctx->has_mesh) return fail(ctx, BGS_ERR_STATE, "no mesh");
+  if (step < 1 || !(dt > 0.0)) return fail(ctx, BGS_ERR_INVALID, "step must be >= 1 and dt > 0");
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  const uint32_t n = ctx->mesh.n_cells;
+  launch_cell_energy(ctx->mesh, ctx->cells, step, dt, ctx->d_mat_E, ctx->d_energy_part, ctx->d_diag,
+                     ctx->n_user, ctx->stream);
+  BGS_LAUNCHED(ctx, 6);
+  launch_scan_counts(ctx->cells.n_em, ctx->cells.n_so, n, ctx->cells.off_new, ctx->d_tile_cells, ctx->stream);
+  BGS_LAUNCHED(ctx, 3);
+  launch_scan_counts(ctx->cells.n_ce, nullptr, n, ctx->cells.off_ce, ctx->d_tile_cells, ctx->stream);
+  BGS_LAUNCHED(ctx, 3);
+  ctx->xs_dirty = false;
+  if (out) {
+    if ((rc = read_diag(ctx))) return rc;
+    unsigned long long offs[2];
+    BGS_CUDA(ctx, cudaMemcpy(&offs[0], ctx->cells.off_new + n, sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    BGS_CUDA(ctx, cudaMemcpy(&offs[1], ctx->cells.off_ce + n, sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    const DeviceDiag &d = *ctx->h_diag;
+    out->total_photon_E = d.total_photon_E;
+    out->emission_E = d.emission_E;
+    out->census_E = d.census_cell_E;
+    out->source_E = d.source_E;
+    out->pre_mat_E = d.pre_mat_E;
+    out->n_new_photons = offs[0];
+    out->n_initial_census = step == 1 ? offs[1] : 0;
+  }
+  return BGS_OK;
+}
+
+int bgs_source(bgs_context *ctx, uint32_t step, double dt) {
+  if (!ctx) return BGS_ERR_INVALID;
+  if (!ctx->has_mesh) return fail(ctx, BGS_ERR_STATE, "no mesh");
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  launch_plan_bank(ctx->mesh, ctx->cells, ctx->d_diag, step, ctx->capacity, ctx->stream);
+  BGS_LAUNCHED(ctx, 1);
+  launch_source(ctx->mesh, ctx->cells, ctx->bank[ctx->cur], ctx->d_diag, ctx->seed, step, dt, ctx->n_sm,
+                ctx->stream);
+  BGS_LAUNCHED(ctx, step == 1 ? 2 : 1);
+  ctx->bank_is_census = false;
+  return BGS_OK;
+}
+
+static int transport_impl(bgs_context *ctx, double next_dt, uint32_t algorithm, bool read_back) {
+  if (algorithm != BGS_HISTORY && algorithm != BGS_EVENT)
+    return fail(ctx, BGS_ERR_INVALID, "unknown transport algorithm %u", algorithm);
+  if (ctx->xs_dirty) {
+    launch_cell_xs(ctx->mesh, ctx->cells, ctx->stream);
+    BGS_LAUNCHED(ctx, 1);
+    ctx->xs_dirty = false;
+  }
+  const uint64_t before = ctx->launches;
+  Bank &from = ctx->bank[ctx->cur];
+  Bank &to = ctx->bank[1 - ctx->cur];
+  launch_bank_bounds(from, ctx->d_maxbits, ctx->d_diag, ctx->n_sm, ctx->stream);
+  BGS_LAUNCHED(ctx, 2);
+  BGS_CUDA(ctx, cudaMemsetAsync(ctx->cells.tally, 0, ctx->mesh.n_cells * sizeof(TallyCell), ctx->stream));
+  k_reset_queue<<<1, 1, 0, ctx->stream>>>(ctx->d_diag);
+  BGS_LAUNCHED(ctx, 1);
+  BGS_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+  launch_transport_history(ctx->mesh, ctx->cells, from, ctx->d_diag, ctx->seed, ctx->tshape, ctx->stream);
+  BGS_LAUNCHED(ctx, 1);
+  BGS_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+  launch_scan_flags(from.desc, CENSUS, (uint32_t)ctx->capacity, &ctx->d_diag->n_bank, ctx->d_off_bank,
+                    ctx->d_tile_bank, ctx->stream);
+  BGS_LAUNCHED(ctx, 3);
+  launch_census(from, to, ctx->d_diag, ctx->d_off_bank, next_dt, ctx->n_sm, ctx->stream);
+  BGS_LAUNCHED(ctx, 2);
+  launch_tally_to_double(ctx->mesh, ctx->cells, ctx->d_diag, ctx->d_abs, ctx->d_track, ctx->stream);
+  BGS_LAUNCHED(ctx, 2);
+  ctx->last_launches = (uint32_t)(ctx->launches - before);
+  ctx->cur = 1 - ctx->cur;
+  ctx->bank_is_census = true;
+  (void)read_back;
+  return BGS_OK;
+}
+
+int bgs_transport(bgs_context *ctx, double next_dt, uint32_t algorithm, bgs_transport_diag *out) {
+  if (!ctx) return BGS_ERR_INVALID;
+  if (!ctx->has_mesh) return fail(ctx, BGS_ERR_STATE, "no mesh");
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  if ((rc = transport_impl(ctx, next_dt, algorithm, out != nullptr))) return rc;
+  if (out) {
+    if ((rc = read_diag(ctx))) return rc;
+    fill_transport_diag(*ctx->h_diag, out);
+    return check_flags(ctx, ctx->h_diag->flags);
+  }
+  return BGS_OK;
+}
+
+int bgs_update_temperature(bgs_context *ctx, double dt, bgs_transport_diag *out) {
+  if (!ctx) return BGS_ERR_INVALID;
+  if (!ctx->has_mesh) return fail(ctx, BGS_ERR_STATE, "no mesh");
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  launch_update_temperature(ctx->mesh, ctx->cells, ctx->d_diag, dt, ctx->d_abs, ctx->d_track,
+                            ctx->d_mat_part, ctx->stream);
+  BGS_LAUNCHED(ctx, 2);
+  if (out) {
+    if ((rc = read_diag(ctx))) return rc;
+    fill_transport_diag(*ctx->h_diag, out);
+    return check_flags(ctx, ctx->h_diag->flags);
+  }
+  return BGS_OK;
+}
+
+int bgs_step(bgs_context *ctx, const bgs_step_params *p, bgs_transport_diag *out) {
+  if (!ctx || !p) return BGS_ERR_INVALID;
+  int rc;
+  if ((rc = bgs_calculate_photon_energy(ctx, p->step, p->dt, nullptr))) return rc;
+  if ((rc = bgs_source(ctx, p->step, p->dt))) return rc;
+  if ((rc = transport_impl(ctx, p->next_dt, p->algorithm, out != nullptr))) return rc;
+  if ((rc = bgs_update_temperature(ctx, p->dt, out))) return rc;
+  return BGS_OK;
+}
+
+int bgs_synchronize(bgs_context *ctx) {
+  if (!ctx) return BGS_ERR_INVALID;
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  if ((rc = read_diag(ctx))) return rc;
+  return check_flags(ctx, ctx->h_diag->flags);
+}
+
+int bgs_bank_size(bgs_context *ctx, uint64_t *n) {
+  if (!ctx || !n) return BGS_ERR_INVALID;
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  if ((rc = read_diag(ctx))) return rc;
+  *n = ctx->bank_is_census ? ctx->h_diag->n_census_in : ctx->h_diag->n_bank;
+  return BGS_OK;
+}
+
+int bgs_get_photons(bgs_context *ctx, uint64_t offset, uint64_t count, const bgs_photons_host *out) {
+  if (!ctx || !out) return BGS_ERR_INVALID;
+  uint64_t n = 0;
+  int rc = bgs_bank_size(ctx, &n);
+  if (rc) return rc;
+  if (offset > n || count > n - offset)
+    return fail(ctx, BGS_ERR_INVALID, "photon range [%llu, %llu) outside a bank of %llu",
+                (unsigned long long)offset, (unsigned long long)(offset + count), (unsigned long long)n);
+  if ((rc = copy_photons(ctx, ctx->bank[ctx->cur], offset, count, out, true))) return rc;
+  BGS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return BGS_OK;
+}
+
+int bgs_set_photons(bgs_context *ctx, uint64_t count, const bgs_photons_host *in) {
+  if (!ctx || !in) return BGS_ERR_INVALID;
+  if (count > ctx->capacity)
+    return fail(ctx, BGS_ERR_CAPACITY, "%llu photons exceed the bank capacity %llu",
+                (unsigned long long)count, ctx->capacity);
+  if (!in->pos_x || !in->pos_y || !in->pos_z || !in->dir_x || !in->dir_y || !in->dir_z || !in->E ||
+      !in->E0 || !in->life_dx || !in->cell || !in->group || !in->rng_stream || !in->rng_counter)
+    return fail(ctx, BGS_ERR_INVALID, "input photons need every state array");
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  Bank &b = ctx->bank[ctx->cur];
+  if ((rc = copy_photons(ctx, b, 0, count, in, false))) return rc;
+  if (!in->descriptor) BGS_CUDA(ctx, cudaMemsetAsync(b.desc, PASS, count, ctx->stream));
+  if (!in->source_type) BGS_CUDA(ctx, cudaMemsetAsync(b.stype, 0, count, ctx->stream));
+  k_set_bank_size<<<1, 1, 0, ctx->stream>>>(ctx->d_diag, count);
+  BGS_LAUNCHED(ctx, 1);
+  BGS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->bank_is_census = false;
+  return BGS_OK;
+}
+
+int bgs_replicated_transport(bgs_context *ctx, uint64_t n, const bgs_photons_host *photons,
+                             double next_dt, uint32_t algorithm, double *rank_abs_E,
+                             double *rank_track_E, const bgs_photons_host *census,
+                             uint64_t census_capacity, uint64_t *n_census, double *census_E,
+                             double *exit_E) {
+  if (!ctx || !photons) return BGS_ERR_INVALID;
+  if (!ctx->has_mesh) return fail(ctx, BGS_ERR_STATE, "no mesh");
+  int rc;
+  if ((rc = bgs_set_photons(ctx, n, photons))) return rc;
+  if ((rc = transport_impl(ctx, next_dt, algorithm, true))) return rc;
+  // end states come back from the bank that was transported
+  const Bank &done = ctx->bank[1 - ctx->cur];
+  bgs_photons_host back = *photons;
+  back.E0 = nullptr;           // unchanged by transport
+  back.rng_stream = nullptr;
+  back.source_type = nullptr;
+  if ((rc = copy_photons(ctx, done, 0, n, &back, true))) return rc;
+  if (rank_abs_E)
+    BGS_CUDA(ctx, cudaMemcpyAsync(rank_abs_E, ctx->d_abs, ctx->mesh.n_cells * sizeof(double),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+  if (rank_track_E)
+    BGS_CUDA(ctx, cudaMemcpyAsync(rank_track_E, ctx->d_track, ctx->mesh.n_cells * sizeof(double),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+  if ((rc = read_diag(ctx))) return rc;
+  const DeviceDiag &d = *ctx->h_diag;
+  if (census_E) *census_E = d.census_E;
+  if (exit_E) *exit_E = d.exit_E;
+  if (n_census) *n_census = d.n_census_out;
+  if ((rc = check_flags(ctx, d.flags))) return rc;
+  if (census) {
+    if (d.n_census_out > census_capacity)
+      return fail(ctx, BGS_ERR_CAPACITY, "census of %llu photons exceeds the buffer of %llu",
+                  d.n_census_out, (unsigned long long)census_capacity);
+    if ((rc = copy_photons(ctx, ctx->bank[ctx->cur], 0, d.n_census_out, census, true))) return rc;
+    BGS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  return BGS_OK;
+}
+
+int bgs_last_transport_ms(bgs_context *ctx, float *ms, uint32_t *kernel_launches) {
+  if (!ctx || !ms) return BGS_ERR_INVALID;
+  BGS_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
+  BGS_CUDA(ctx, cudaEventElapsedTime(ms, ctx->ev0, ctx->ev1));
+  if (kernel_launches) *kernel_launches = ctx->last_launches;
+  return BGS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,210 @@
+// Internal device data model and helpers of the GB300 replicated IMC step.
+//
+// Layout in HBM (one context):
+//   mesh     : plane arrays x[ngx+1], y[ngy+1], z[ngz+1]; cell_region[n];
+//              region table (n_regions x 8 doubles)
+//   cells    : structure of arrays of doubles, one entry per cell
+//              (T_e, T_r initial, T_s, op_a, op_s, f, emission/census/source E,
+//              T_r diagnostic) plus the transport table XS[n] (32 B per cell)
+//   tallies  : TallyCell[n] = 128-bit fixed-point absorbed and track energy
+//              (32 B per cell), order-independent integer sums
+//   photons  : two banks, each a structure of arrays sized to the capacity
+//   counts   : per-cell photon counts and their exclusive prefix sums
+//   diag     : one DeviceDiag (step scalars, flags)
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace bgs {
+
+// Constants namespace (constants.h:16-24)
+constexpr double kPi = 3.1415926535897932384626433832795;
+constexpr double kC = 299.792458;
+constexpr double kA = 0.01372;
+constexpr double kCutoff = 0.01;
+
+enum : int { REFLECT = 0, VACUUM = 1, ELEMENT = 2, SOURCE = 3, PROCESSOR = 4 };
+enum : uint8_t { EXIT = 0, PASS = 1, CENSUS = 2, SCATTER = 3, KILLED = 4, BOUND = 5 };
+
+// device-side check bits (DeviceDiag::flags)
+enum : uint32_t {
+  FLAG_CAPACITY = 1u << 0,      // bank would overflow: no photons made
+  FLAG_TALLY_RANGE = 1u << 1,   // a tally contribution outside the fixed-point range
+  FLAG_SEGMENT_LIMIT = 1u << 2, // a history exceeded the segment limit and was killed
+  FLAG_BAD_CELL = 1u << 3,      // a photon referenced a cell outside the mesh
+  FLAG_NAN = 1u << 4,           // a non-finite tally contribution was dropped
+};
+
+// Upper bound on loop trips of one history inside one step; a history that
+// reaches it is ended as KILLED and FLAG_SEGMENT_LIMIT is raised.
+constexpr uint32_t kMaxSegmentsPerHistory = 100000000u;
+
+// Per-cell transport coefficients, derived each step from op_a, op_s, f.
+// Each is formed with the exact expression transport_photon evaluates
+// (history_based_transport.h:56-59, :74, :77, :97), so results are bitwise
+// those of the upstream loop:
+//   sig_eff  = (1 - f)*sigma_a + sigma_s   (effective scattering opacity)
+//   neg_saf  = -sigma_a * f                (exponent rate, negated)
+//   saf      =  sigma_a * f                (track-length divisor)
+//   p_scat   = sigma_s / sig_eff           (physical-scatter probability)
+struct __align__(32) CellXS {
+  double sig_eff, neg_saf, saf, p_scat;
+};
+
+// 128-bit fixed-point tally cell: value = (hi*2^64 + lo) * 2^-scale.
+struct __align__(32) TallyCell {
+  unsigned long long abs_lo, abs_hi, trk_lo, trk_hi;
+};
+
+// Photon bank: structure of arrays (photon.h:172-181 fields).
+struct Bank {
+  double *px, *py, *pz, *dx, *dy, *dz, *E, *E0, *life;
+  uint32_t *cell, *group;
+  uint8_t *desc, *stype;
+  unsigned long long *stream, *ctr;
+};
+
+struct MeshDev {
+  uint32_t ngx, ngy, ngz, n_groups;
+  uint32_t n_cells, n_regions;
+  const double *x, *y, *z;
+  const uint32_t *region;
+  const double *regions;  // n_regions x 8
+  int bc[6];
+  double T_source;
+};
+
+struct CellsDev {
+  double *T_e, *T_r, *T_s, *op_a, *op_s, *f, *em_E, *ce_E, *so_E, *T_r_diag;
+  double *group_v;        // op_a * (1/(op_a*N)): one CDF step of sample_emission_group
+  CellXS *xs;
+  TallyCell *tally;
+  int8_t *source_face;    // Cell::get_source_face (cell.h:69-76), -1 if none
+  uint32_t *n_em, *n_so, *n_ce;          // photons per cell
+  unsigned long long *off_new, *off_ce;  // exclusive prefix sums (n+1 entries)
+};
+
+// Scalars of one step kept on the device (so a step never waits for the host).
+struct DeviceDiag {
+  double total_photon_E, emission_E, census_cell_E, source_E, pre_mat_E;
+  double census_E_in;                 // energy of the census carried into the step
+  unsigned long long n_new, n_init_census, n_census_in, n_bank;
+  unsigned long long n_census_out, n_segments;
+  unsigned long long work_counter;    // transport work queue head
+  unsigned long long census_counter;  // (unused by the scan path)
+  unsigned long long sum_census[2], sum_exit[2], sum_abs[2];  // 128-bit fixed point
+  double census_E, exit_E, absorbed_E, post_mat_E;
+  int scale_abs, scale_track;         // fixed-point exponents of this step
+  uint32_t flags;
+  uint32_t serial_needed;             // a photon count needed the serial energy sum
+};
+
+// ------------------------------------------------------------------ RNG
+// Threefry2x64-20 (Salmon et al., SC'11), key (stream, 0), counter
+// (ctr, seed << 32): the generator RNG::generate_random_number draws from
+// (RNG.h:262-285, threefry.h:190-293).
+__device__ __forceinline__ unsigned long long rotl64(unsigned long long x, int r) {
+  return (x << r) | (x >> (64 - r));
+}
+
+__device__ __forceinline__ unsigned long long threefry2x64_20_w0(unsigned long long c0,
+                                                                 unsigned long long c1,
+                                                                 unsigned long long k0) {
+  const unsigned long long k2 = 0x1BD11BDAA9FC1A22ULL ^ k0;  // k1 = 0
+  unsigned long long x0 = c0 + k0, x1 = c1;
+#define BGS_MIX(R) { x0 += x1; x1 = rotl64(x1, R); x1 ^= x0; }
+  BGS_MIX(16) BGS_MIX(42) BGS_MIX(12) BGS_MIX(31)
+  x0 += 0;  x1 += k2 + 1ULL;   // injection 1: ks[1], ks[2] + 1
+  BGS_MIX(16) BGS_MIX(32) BGS_MIX(24) BGS_MIX(21)
+  x0 += k2; x1 += k0 + 2ULL;   // injection 2: ks[2], ks[0] + 2
+  BGS_MIX(16) BGS_MIX(42) BGS_MIX(12) BGS_MIX(31)
+  x0 += k0; x1 += 3ULL;        // injection 3: ks[0], ks[1] + 3
+  BGS_MIX(16) BGS_MIX(32) BGS_MIX(24) BGS_MIX(21)
+  x0 += 0;  x1 += k2 + 4ULL;   // injection 4: ks[1], ks[2] + 4
+  BGS_MIX(16) BGS_MIX(42) BGS_MIX(12) BGS_MIX(31)
+  x0 += k2;                    // injection 5: ks[2] (x1 is not needed)
+#undef BGS_MIX
+  return x0;
+}
+
+// u01fixedpt<double, uint64_t> (RNG.h:202-238): ((w >> 11) | 1) * 2^-53,
+// assembled from integer bits (exact; no floating-point conversion needed).
+__device__ __forceinline__ double u01_from_bits(unsigned long long w) {
+  const unsigned long long m = (w >> 11) | 1ULL;     // 1 <= m < 2^53, odd
+  const int s = __clzll(m) - 11;                     // shift to put the top bit at 52
+  const unsigned long long mant = (m << s) & 0x000FFFFFFFFFFFFFULL;
+  const unsigned long long expo = (unsigned long long)(1023 - 1 - s);  // value in [2^-1-s, 2^-s)
+  return __longlong_as_double((long long)((expo << 52) | mant));
+}
+
+struct Rng {
+  unsigned long long stream, ctr, hi;  // hi = seed << 32
+  __device__ __forceinline__ double next() {
+    const double u = u01_from_bits(threefry2x64_20_w0(ctr, hi, stream));
+    ++ctr;
+    return u;
+  }
+};
+
+// ------------------------------------------------------ fixed point
+// x >= 0 to a 128-bit integer floor(x * 2^scale); contributions far below
+// the tally's resolution truncate.  Returns false if out of range.
+__device__ __forceinline__ bool to_fixed128(double x, int scale, unsigned long long &lo,
+                                            unsigned long long &hi) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((bits >> 52) & 0x7FF);
+  lo = 0;
+  hi = 0;
+  if (bits >> 63) return x == 0.0;   // negative (or -0.0)
+  if (e == 0x7FF) return false;      // inf / nan
+  if (e == 0) return true;           // zero or subnormal: below resolution
+  const unsigned long long m = (bits & 0x000FFFFFFFFFFFFFULL) | 0x0010000000000000ULL;
+  const int sh = e - 1075 + scale;   // x = m * 2^(e-1075)
+  if (sh >= 0) {
+    if (sh > 74) return false;       // would not fit in 128 bits
+    if (sh == 0) { lo = m; }
+    else if (sh < 64) { lo = m << sh; hi = m >> (64 - sh); }
+    else { hi = m << (sh - 64); }
+  } else {
+    if (sh > -64) lo = m >> (-sh);
+  }
+  return true;
+}
+
+__device__ __forceinline__ void atomic_add128(unsigned long long *lo_p, unsigned long long *hi_p,
+                                              unsigned long long lo, unsigned long long hi) {
+  if (lo) {
+    const unsigned long long old = atomicAdd(lo_p, lo);
+    if (old + lo < old) hi += 1ULL;  // carry out of the low word
+  }
+  if (hi) atomicAdd(hi_p, hi);
+}
+
+__host__ __device__ __forceinline__ double from_fixed128(unsigned long long lo, unsigned long long hi,
+                                                         int scale) {
+  const double v = (double)hi * 18446744073709551616.0 + (double)lo;
+#ifdef __CUDA_ARCH__
+  return scalbn(v, -scale);
+#else
+  return __builtin_scalbn(v, -scale);
+#endif
+}
+
+// exponent such that bound * 2^scale <= 2^118 (ten bits of headroom below 2^128)
+__device__ __forceinline__ int fixed_scale_for(double bound) {
+  if (!(bound > 0.0)) return 0;
+  int e;
+  frexp(bound, &e);  // bound < 2^e
+  return 118 - e;
+}
+
+// ------------------------------------------------------ photon counts
+// photons made for one cell energy (source.h:229-243): at least one
+__device__ __forceinline__ uint32_t photons_for(unsigned long long n_user, double E, double total_E) {
+  if (!(E > 0.0)) return 0u;
+  const uint32_t t = (uint32_t)(int)((double)n_user * E / total_E);
+  return t == 0u ? 1u : t;
+}
+
+}  // namespace bgs

@@ -1,0 +1,74 @@
+// Device helpers shared by the kernels and the host launcher declarations.
+#pragma once
+
+#include "bgs_internal.cuh"
+
+namespace bgs {
+
+// node array of cell g (cell.h:325): (x_lo, x_hi, y_lo, y_hi, z_lo, z_hi)
+__device__ __forceinline__ void cell_nodes(const MeshDev &m, uint32_t g, double n[6]) {
+  const uint32_t i = g % m.ngx, j = (g / m.ngx) % m.ngy, k = g / (m.ngx * m.ngy);
+  n[0] = m.x[i];
+  n[1] = m.x[i + 1];
+  n[2] = m.y[j];
+  n[3] = m.y[j + 1];
+  n[4] = m.z[k];
+  n[5] = m.z[k + 1];
+}
+
+// Cell::get_volume (cell.h:188-191)
+__device__ __forceinline__ double cell_volume(const double n[6]) {
+  return (n[1] - n[0]) * (n[3] - n[2]) * (n[5] - n[4]);
+}
+
+// per-cell transport coefficients (see CellXS) and the CDF step of
+// sample_emission_group's walk, op_a(g) * 1/(op_a(0)*N) with all groups
+// equal (sampling_functions.h:132-135, cell.h:260-266)
+__device__ __forceinline__ void set_cell_xs(const CellsDev &c, uint32_t g, double op_a, double op_s,
+                                            double f, uint32_t n_groups) {
+  CellXS x;
+  x.sig_eff = (1.0 - f) * op_a + op_s;
+  x.neg_saf = -op_a * f;
+  x.saf = op_a * f;
+  x.p_scat = op_s / ((1.0 - f) * op_a + op_s);
+  c.xs[g] = x;
+  const double norm_factor = 1.0 / (op_a * (double)n_groups);
+  c.group_v[g] = op_a * norm_factor;
+}
+
+// ---------------------------------------------------------------- launchers
+void launch_init_cells(const MeshDev &m, const CellsDev &c, cudaStream_t s);
+uint32_t energy_parts(uint32_t n_cells);
+void launch_cell_energy(const MeshDev &m, const CellsDev &c, uint32_t step, double dt, double *mat_E,
+                        double *part, DeviceDiag *d, unsigned long long n_user, cudaStream_t s);
+void launch_cell_xs(const MeshDev &m, const CellsDev &c, cudaStream_t s);
+uint32_t scan_tiles_needed(uint64_t n);
+void launch_scan_counts(const uint32_t *cnt, const uint32_t *cnt2, uint32_t n,
+                        unsigned long long *out, unsigned long long *tile_sum, cudaStream_t s);
+void launch_scan_flags(const uint8_t *desc, uint8_t want, uint32_t capacity,
+                       const unsigned long long *n_dev, unsigned long long *out,
+                       unsigned long long *tile_sum, cudaStream_t s);
+void launch_bank_bounds(const Bank &b, unsigned long long *max_bits, DeviceDiag *d, int n_sm,
+                        cudaStream_t s);
+void launch_tally_to_double(const MeshDev &m, const CellsDev &c, DeviceDiag *d, double *abs_out,
+                           double *track_out, cudaStream_t s);
+void launch_update_temperature(const MeshDev &m, const CellsDev &c, DeviceDiag *d, double dt,
+                               const double *abs_in, const double *track_in, double *mat_part,
+                               cudaStream_t s);
+uint32_t update_temperature_parts(uint32_t n_cells);
+
+void launch_plan_bank(const MeshDev &m, const CellsDev &c, DeviceDiag *d, uint32_t step,
+                      unsigned long long capacity, cudaStream_t s);
+void launch_source(const MeshDev &m, const CellsDev &c, const Bank &b, DeviceDiag *d, uint32_t seed,
+                   uint32_t step, double dt, int n_sm, cudaStream_t s);
+
+struct TransportLaunch {
+  int blocks, threads;
+};
+TransportLaunch transport_launch_shape(int n_sm);
+void launch_transport_history(const MeshDev &m, const CellsDev &c, const Bank &b, DeviceDiag *d,
+                              uint32_t seed, const TransportLaunch &shape, cudaStream_t s);
+void launch_census(const Bank &from, const Bank &to, DeviceDiag *d, const unsigned long long *off,
+                   double next_dt, int n_sm, cudaStream_t s);
+
+}  // namespace bgs

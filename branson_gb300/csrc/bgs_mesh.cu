@@ -1,0 +1,497 @@
+// Per-cell physics of the replicated step: opacity / Fleck factor / source
+// energies (Mesh::calculate_photon_energy, mesh.h:237-323), photon counts
+// and their prefix sums (source.h:225-245), and the tally reduce fused with
+// the temperature update (replicated_driver.h:90-96 + Mesh::update_temperature,
+// mesh.h:327-423).
+//
+// All of this is O(cells) work that is HBM/latency bound and small next to
+// transport; the one serial piece is the cell-order floating-point sum of the
+// source energies, kept serial because the photon counts int(n*E/total)
+// depend on its exact rounding.
+#include "bgs_kernels.cuh"
+
+namespace bgs {
+
+// ---------------------------------------------------------------------------
+// Cell::get_source_face over the structured mesh (cell.h:69-76): the first
+// face (X-, X+, Y-, Y+, Z-, Z+) that is a domain face with a SOURCE condition.
+__global__ void k_init_cells(MeshDev m, CellsDev c) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= m.n_cells) return;
+  const uint32_t i = g % m.ngx, j = (g / m.ngx) % m.ngy, k = g / (m.ngx * m.ngy);
+  const bool at_face[6] = {i == 0, i + 1 == m.ngx, j == 0, j + 1 == m.ngy, k == 0, k + 1 == m.ngz};
+  int sf = -1;
+  for (int f = 0; f < 6; ++f)
+    if (at_face[f] && m.bc[f] == SOURCE) { sf = f; break; }
+  c.source_face[g] = (int8_t)sf;
+  const double *r = m.regions + 8 * (size_t)m.region[g];
+  c.T_e[g] = r[6];   // Mesh::initialize_physical_properties (mesh.h:426-439)
+  c.T_r[g] = r[7];
+  c.T_s[g] = sf != -1 ? m.T_source : 0.0;
+}
+
+// Cell::get_face_area (cell.h:83-100)
+__device__ __forceinline__ double face_area(const double n[6], int face) {
+  if (face == 0 || face == 1) return __dmul_rn(__dsub_rn(n[3], n[2]), __dsub_rn(n[5], n[4]));
+  if (face == 2 || face == 3) return __dmul_rn(__dsub_rn(n[1], n[0]), __dsub_rn(n[5], n[4]));
+  if (face == 4 || face == 5) return __dmul_rn(__dsub_rn(n[1], n[0]), __dsub_rn(n[3], n[2]));
+  return -1.0;
+}
+
+// Mesh::calculate_photon_energy per cell (mesh.h:253-287), one rank
+// (replicated factor 1).  Also derives the transport table.
+__global__ void k_cell_energy(MeshDev m, CellsDev c, uint32_t step, double dt, double *mat_E) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= m.n_cells) return;
+  double n[6];
+  cell_nodes(m, g, n);
+  const double vol = cell_volume(n);
+  const double *r = m.regions + 8 * (size_t)m.region[g];
+  const double cV = r[0], rho = r[1], A = r[2], B = r[3], Cx = r[4], S = r[5];
+  const double T = c.T_e[g], Tr = c.T_r[g], Ts = c.T_s[g];
+  const double rf = 1.0;
+  const double op_a = A + B * pow(T, Cx);
+  const double op_s = S;
+  const double f = 1.0 / (1.0 + dt * op_a * kC * (4.0 * kA * pow(T, 3.0) / (cV * rho)));
+  c.op_a[g] = op_a;
+  c.op_s[g] = op_s;
+  c.f[g] = f;
+  c.em_E[g] = rf * dt * vol * f * op_a * kA * kC * pow(T, 4.0);
+  c.ce_E[g] = (step > 1) ? 0.0 : rf * vol * kA * pow(Tr, 4.0);
+  c.so_E[g] = rf * 0.25 * kA * kC * face_area(n, c.source_face[g]) * pow(Ts, 4.0) * dt;
+  mat_E[g] = T * cV * vol * rho;
+  set_cell_xs(c, g, op_a, op_s, f, m.n_groups);
+}
+
+// Transport table from op_a, op_s, f already in the cell arrays (the
+// drop-in path, where the caller supplies the opacities).
+__global__ void k_cell_xs(MeshDev m, CellsDev c) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= m.n_cells) return;
+  set_cell_xs(c, g, c.op_a[g], c.op_s[g], c.f[g], m.n_groups);
+}
+
+// The cell-order sums of calculate_photon_energy (mesh.h:282-287).  The
+// upstream total is a left-to-right floating-point sum, and the photon
+// counts int(n_user*E/total) (source.h:229-243) depend on its rounding.  A
+// serial FP64 chain is very slow on one GPU lane, so the total is first
+// formed by a deterministic tree sum; every cell count is then checked
+// against the rounding-error bound of the serial sum, and only if some count
+// could differ (an integer inside the error window of n_user*E/total) does
+// the serial sum run (k_serial_total).  Either way the counts equal the
+// upstream ones.
+constexpr int kSumThreads = 256;
+
+__global__ void __launch_bounds__(kSumThreads) k_energy_partials(MeshDev m, CellsDev c, const double *mat_E,
+                                                                 double *part) {
+  __shared__ double s[5][kSumThreads];
+  const uint32_t g = blockIdx.x * kSumThreads + threadIdx.x;
+  double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  if (g < m.n_cells) {
+    v[0] = c.so_E[g] + c.ce_E[g] + c.em_E[g];  // the upstream per-cell term
+    v[1] = c.em_E[g];
+    v[2] = c.ce_E[g];
+    v[3] = c.so_E[g];
+    v[4] = mat_E[g];
+  }
+  for (int q = 0; q < 5; ++q) s[q][threadIdx.x] = v[q];
+  __syncthreads();
+  for (int o = kSumThreads / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < (unsigned)o)
+      for (int q = 0; q < 5; ++q) s[q][threadIdx.x] += s[q][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x < 5) part[5 * (size_t)blockIdx.x + threadIdx.x] = s[threadIdx.x][0];
+}
+
+__global__ void k_energy_finish(const double *part, uint32_t n_parts, DeviceDiag *d) {
+  // one warp: lane q < 5 sums column q in block order (deterministic)
+  const int q = threadIdx.x;
+  if (q >= 5) return;
+  double acc = 0.0;
+  for (uint32_t b = 0; b < n_parts; ++b) acc += part[5 * (size_t)b + q];
+  if (q == 0) { d->total_photon_E = acc; d->serial_needed = 0; }
+  if (q == 1) d->emission_E = acc;
+  if (q == 2) d->census_cell_E = acc;
+  if (q == 3) d->source_E = acc;
+  if (q == 4) d->pre_mat_E = acc;
+}
+
+// could int(n_user*E/total_serial) differ from int(n_user*E/total_tree)?
+__device__ __forceinline__ bool count_ambiguous(unsigned long long n_user, double E, double total,
+                                                double window) {
+  if (!(E > 0.0)) return false;
+  const double q = (double)n_user * E / total;
+  const double lo = q - q * window, hi = q + q * window;
+  if (hi < 2.0) return false;  // counts 0 and 1 both become one photon
+  return floor(lo) != floor(hi);
+}
+
+__global__ void k_energy_check(MeshDev m, CellsDev c, DeviceDiag *d, unsigned long long n_user,
+                               uint32_t step) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= m.n_cells) return;
+  const double total = d->total_photon_E;
+  // |serial - exact| <= (n-1) u sum, |tree - exact| <= (log2 n + 1) u sum,
+  // plus the rounding of n*E/total: a window of (n + 64) u, doubled
+  const double window = 2.0 * ((double)m.n_cells + 64.0) * 1.1102230246251565e-16;
+  bool amb = count_ambiguous(n_user, c.em_E[g], total, window) ||
+             count_ambiguous(n_user, c.so_E[g], total, window) ||
+             (step == 1 && count_ambiguous(n_user, c.ce_E[g], total, window));
+  if (amb) d->serial_needed = 1;
+}
+
+// the upstream serial sum, run only when a count is ambiguous; one block
+// stages the per-cell terms in shared memory, thread 0 keeps the add chain
+__global__ void k_serial_total(MeshDev m, CellsDev c, DeviceDiag *d) {
+  if (!d->serial_needed) return;
+  constexpr int kChunk = 2048;
+  __shared__ double s_t[kChunk];
+  double total = 0.0;
+  for (uint32_t base = 0; base < m.n_cells; base += kChunk) {
+    const uint32_t cnt = min((uint32_t)kChunk, m.n_cells - base);
+    for (uint32_t t = threadIdx.x; t < cnt; t += blockDim.x) {
+      const uint32_t g = base + t;
+      s_t[t] = c.so_E[g] + c.ce_E[g] + c.em_E[g];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+      for (uint32_t t = 0; t < cnt; ++t) total += s_t[t];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) d->total_photon_E = total;
+}
+
+// photons per cell for emission, boundary source and (step 1) initial census
+__global__ void k_counts(MeshDev m, CellsDev c, const DeviceDiag *d, unsigned long long n_user,
+                         uint32_t step) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= m.n_cells) return;
+  const double total = d->total_photon_E;
+  c.n_em[g] = photons_for(n_user, c.em_E[g], total);
+  c.n_so[g] = photons_for(n_user, c.so_E[g], total);
+  c.n_ce[g] = step == 1 ? photons_for(n_user, c.ce_E[g], total) : 0u;
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive prefix sum of uint32 counts into uint64 offsets (n+1 entries),
+// three passes: per-block scan, scan of block totals, add.
+constexpr int kScanThreads = 512;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+template <typename Pred>
+__device__ __forceinline__ void scan_tile(uint32_t n, uint32_t tile, Pred value,
+                                          unsigned long long *out, unsigned long long *tile_sum) {
+  __shared__ unsigned long long s_warp[kScanThreads / 32];
+  const uint32_t base = tile * kScanTile + threadIdx.x * kScanItems;
+  unsigned long long v[kScanItems];
+  unsigned long long run = 0;
+#pragma unroll
+  for (int q = 0; q < kScanItems; ++q) {
+    const uint32_t idx = base + q;
+    v[q] = idx < n ? (unsigned long long)value(idx) : 0ULL;
+    run += v[q];
+  }
+  // inclusive warp scan of the per-thread totals
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long incl = run;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    unsigned long long w = lane < kScanThreads / 32 ? s_warp[lane] : 0ULL;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long t = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += t;
+    }
+    if (lane < kScanThreads / 32) s_warp[lane] = w;
+  }
+  __syncthreads();
+  unsigned long long excl = incl - run + (warp > 0 ? s_warp[warp - 1] : 0ULL);
+#pragma unroll
+  for (int q = 0; q < kScanItems; ++q) {
+    const uint32_t idx = base + q;
+    if (idx < n) out[idx] = excl;
+    excl += v[q];
+  }
+  if (threadIdx.x == kScanThreads - 1) tile_sum[tile] = excl;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_counts(const uint32_t *cnt, const uint32_t *cnt2,
+                                                              uint32_t n, unsigned long long *out,
+                                                              unsigned long long *tile_sum) {
+  if (cnt2)
+    scan_tile(n, blockIdx.x, [cnt, cnt2](uint32_t i) { return cnt[i] + cnt2[i]; }, out, tile_sum);
+  else
+    scan_tile(n, blockIdx.x, [cnt](uint32_t i) { return cnt[i]; }, out, tile_sum);
+}
+
+// flags of a bank whose live length *n_dev is only known on the device; the
+// grid covers the capacity and tiles past the end exit at once
+__global__ void __launch_bounds__(kScanThreads) k_scan_flags(const uint8_t *desc, uint8_t want,
+                                                             const unsigned long long *n_dev,
+                                                             unsigned long long *out,
+                                                             unsigned long long *tile_sum) {
+  const unsigned long long n = *n_dev;
+  if ((unsigned long long)blockIdx.x * kScanTile >= n) {
+    if (threadIdx.x == 0) tile_sum[blockIdx.x] = 0ULL;
+    return;
+  }
+  scan_tile((uint32_t)n, blockIdx.x, [desc, want](uint32_t i) { return desc[i] == want ? 1u : 0u; },
+            out, tile_sum);
+}
+
+// exclusive scan of tile sums in one block (sequential over chunks)
+__global__ void __launch_bounds__(1024) k_scan_tiles(unsigned long long *tile_sum, uint32_t n_tiles,
+                                                     unsigned long long *total_out) {
+  __shared__ unsigned long long s[1024];
+  unsigned long long carry = 0;
+  for (uint32_t base = 0; base < n_tiles; base += 1024) {
+    const uint32_t i = base + threadIdx.x;
+    const unsigned long long v = i < n_tiles ? tile_sum[i] : 0ULL;
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+      const unsigned long long t = threadIdx.x >= (unsigned)o ? s[threadIdx.x - o] : 0ULL;
+      __syncthreads();
+      s[threadIdx.x] += t;
+      __syncthreads();
+    }
+    if (i < n_tiles) tile_sum[i] = carry + s[threadIdx.x] - v;
+    const unsigned long long chunk_total = s[1023];
+    __syncthreads();
+    carry += chunk_total;
+  }
+  if (threadIdx.x == 0 && total_out) *total_out = carry;
+}
+
+__global__ void k_scan_add(unsigned long long *out, uint32_t n, const unsigned long long *n_dev,
+                           const unsigned long long *tile_sum, const unsigned long long *total) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n_dev) n = (uint32_t)*n_dev;
+  if (i < n) out[i] += tile_sum[i / kScanTile];
+  if (i == 0) out[n] = *total;
+}
+
+// ---------------------------------------------------------------------------
+// Fixed-point scales for a bank of photons: bounds from the largest photon
+// energy and the longest remaining flight (order-independent maxima, so the
+// scales and hence the tallies are deterministic).
+__global__ void k_bank_bounds(Bank b, const DeviceDiag *d, unsigned long long *max_bits) {
+  const unsigned long long n = d->n_bank;
+  unsigned long long mE = 0, mL = 0;
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    const double e = fabs(b.E[i]), l = fabs(b.life[i]);
+    mE = max(mE, (unsigned long long)__double_as_longlong(e));
+    mL = max(mL, (unsigned long long)__double_as_longlong(l));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mE = max(mE, __shfl_down_sync(0xffffffffu, mE, o));
+    mL = max(mL, __shfl_down_sync(0xffffffffu, mL, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&max_bits[0], mE);
+    atomicMax(&max_bits[1], mL);
+  }
+}
+
+__global__ void k_set_scales(DeviceDiag *d, const unsigned long long *max_bits) {
+  const double maxE = __longlong_as_double((long long)max_bits[0]);
+  const double maxL = __longlong_as_double((long long)max_bits[1]);
+  const double n = (double)(d->n_bank > 0 ? d->n_bank : 1ULL);
+  // absorbed energy of a history <= its starting energy; its track-length
+  // tally <= starting energy * remaining flight (transport_photon :74-79)
+  const double bound_abs = 2.0 * maxE * n + 1e-300;
+  const double bound_trk = 2.0 * maxE * fmax(maxL, 1e-300) * n + 1e-300;
+  d->scale_abs = fixed_scale_for(bound_abs);
+  d->scale_track = fixed_scale_for(bound_trk);
+}
+
+// ---------------------------------------------------------------------------
+// 128-bit values as three 43-bit limbs so block sums of up to 2^21 terms
+// are exact in 64-bit adds.
+struct Limbs { unsigned long long a0, a1, a2; };
+__device__ __forceinline__ Limbs limbs_of(unsigned long long lo, unsigned long long hi) {
+  const unsigned long long M = (1ULL << 43) - 1ULL;
+  return {lo & M, ((lo >> 43) | (hi << 21)) & M, hi >> 22};
+}
+__device__ __forceinline__ void limbs_to128(const Limbs &l, unsigned long long &lo,
+                                            unsigned long long &hi) {
+  // value = a0 + a1*2^43 + a2*2^86
+  lo = l.a0;
+  hi = 0;
+  const unsigned long long t1 = l.a1 << 43;
+  const unsigned long long o = lo;
+  lo += t1;
+  hi += (lo < o) ? 1ULL : 0ULL;
+  hi += l.a1 >> 21;
+  hi += l.a2 << 22;
+}
+
+__device__ __forceinline__ Limbs block_sum_limbs(Limbs v) {
+  __shared__ unsigned long long s[3][32];
+  for (int o = 16; o > 0; o >>= 1) {
+    v.a0 += __shfl_down_sync(0xffffffffu, v.a0, o);
+    v.a1 += __shfl_down_sync(0xffffffffu, v.a1, o);
+    v.a2 += __shfl_down_sync(0xffffffffu, v.a2, o);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) { s[0][warp] = v.a0; s[1][warp] = v.a1; s[2][warp] = v.a2; }
+  __syncthreads();
+  Limbs r{0, 0, 0};
+  if (warp == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    r.a0 = lane < nw ? s[0][lane] : 0ULL;
+    r.a1 = lane < nw ? s[1][lane] : 0ULL;
+    r.a2 = lane < nw ? s[2][lane] : 0ULL;
+    for (int o = 16; o > 0; o >>= 1) {
+      r.a0 += __shfl_down_sync(0xffffffffu, r.a0, o);
+      r.a1 += __shfl_down_sync(0xffffffffu, r.a1, o);
+      r.a2 += __shfl_down_sync(0xffffffffu, r.a2, o);
+    }
+  }
+  return r;  // valid in thread 0
+}
+
+__device__ void block_add128(unsigned long long lo, unsigned long long hi, unsigned long long *dst) {
+  Limbs t = block_sum_limbs(limbs_of(lo, hi));
+  if (threadIdx.x == 0) {
+    unsigned long long l, h;
+    limbs_to128(t, l, h);
+    atomic_add128(&dst[0], &dst[1], l, h);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Tally -> double per cell (the values replicated_transport copies out to
+// rank_abs_E / rank_track_E, replicated_transport.h:135-140) with the total
+// absorbed energy summed exactly from the fixed-point integers.
+__global__ void k_tally_to_double(MeshDev m, CellsDev c, DeviceDiag *d, double *abs_out,
+                                  double *track_out) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long alo = 0, ahi = 0;
+  if (g < m.n_cells) {
+    const TallyCell t = c.tally[g];
+    abs_out[g] = from_fixed128(t.abs_lo, t.abs_hi, d->scale_abs);
+    track_out[g] = from_fixed128(t.trk_lo, t.trk_hi, d->scale_track);
+    alo = t.abs_lo;
+    ahi = t.abs_hi;
+  }
+  block_add128(alo, ahi, d->sum_abs);
+}
+
+__global__ void k_tally_total(DeviceDiag *d) {
+  d->absorbed_E = from_fixed128(d->sum_abs[0], d->sum_abs[1], d->scale_abs);
+}
+
+// Mesh::update_temperature (mesh.h:349-362) per cell and a deterministic
+// block-ordered sum of the post-step material energy.
+__global__ void k_update_temperature(MeshDev m, CellsDev c, double dt, const double *abs_in,
+                                     const double *track_in, double *mat_part) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  double matE = 0.0;
+  if (g < m.n_cells) {
+    double n[6];
+    cell_nodes(m, g, n);
+    const double vol = cell_volume(n);
+    const double *r = m.regions + 8 * (size_t)m.region[g];
+    const double cV = r[0], rho = r[1];
+    const double T = c.T_e[g];
+    const double T_new = T + (abs_in[g] - c.em_E[g]) / (cV * vol * rho);
+    c.T_r_diag[g] = pow(track_in[g] / (vol * dt * kA * kC), 0.25);
+    c.T_e[g] = T_new;
+    matE = T_new * cV * vol * rho;
+  }
+  __shared__ double s[256];
+  s[threadIdx.x] = matE;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < (unsigned)o) s[threadIdx.x] += s[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) mat_part[blockIdx.x] = s[0];
+}
+
+__global__ void k_finish_temperature(DeviceDiag *d, const double *mat_part, uint32_t n_parts) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double s = 0.0;
+  for (uint32_t i = 0; i < n_parts; ++i) s += mat_part[i];
+  d->post_mat_E = s;
+}
+
+// ---------------------------------------------------------------------------
+// host launchers
+void launch_init_cells(const MeshDev &m, const CellsDev &c, cudaStream_t s) {
+  k_init_cells<<<(m.n_cells + 255) / 256, 256, 0, s>>>(m, c);
+}
+
+uint32_t energy_parts(uint32_t n_cells) { return (n_cells + kSumThreads - 1) / kSumThreads; }
+
+void launch_cell_energy(const MeshDev &m, const CellsDev &c, uint32_t step, double dt, double *mat_E,
+                        double *part, DeviceDiag *d, unsigned long long n_user, cudaStream_t s) {
+  const uint32_t blocks = (m.n_cells + 255) / 256;
+  const uint32_t parts = energy_parts(m.n_cells);
+  k_cell_energy<<<blocks, 256, 0, s>>>(m, c, step, dt, mat_E);
+  k_energy_partials<<<parts, kSumThreads, 0, s>>>(m, c, mat_E, part);
+  k_energy_finish<<<1, 32, 0, s>>>(part, parts, d);
+  k_energy_check<<<blocks, 256, 0, s>>>(m, c, d, n_user, step);
+  k_serial_total<<<1, 256, 0, s>>>(m, c, d);
+  k_counts<<<blocks, 256, 0, s>>>(m, c, d, n_user, step);
+}
+
+void launch_cell_xs(const MeshDev &m, const CellsDev &c, cudaStream_t s) {
+  k_cell_xs<<<(m.n_cells + 255) / 256, 256, 0, s>>>(m, c);
+}
+
+uint32_t scan_tiles_needed(uint64_t n) { return (uint32_t)((n + kScanTile - 1) / kScanTile); }
+
+void launch_scan_counts(const uint32_t *cnt, const uint32_t *cnt2, uint32_t n, unsigned long long *out,
+                        unsigned long long *tile_sum, cudaStream_t s) {
+  const uint32_t tiles = scan_tiles_needed(n) > 0 ? scan_tiles_needed(n) : 1;
+  k_scan_counts<<<tiles, kScanThreads, 0, s>>>(cnt, cnt2, n, out, tile_sum);
+  k_scan_tiles<<<1, 1024, 0, s>>>(tile_sum, tiles, tile_sum + tiles);
+  k_scan_add<<<(n + 256) / 256, 256, 0, s>>>(out, n, nullptr, tile_sum, tile_sum + tiles);
+}
+
+void launch_scan_flags(const uint8_t *desc, uint8_t want, uint32_t capacity,
+                       const unsigned long long *n_dev, unsigned long long *out,
+                       unsigned long long *tile_sum, cudaStream_t s) {
+  const uint32_t tiles = scan_tiles_needed(capacity) > 0 ? scan_tiles_needed(capacity) : 1;
+  k_scan_flags<<<tiles, kScanThreads, 0, s>>>(desc, want, n_dev, out, tile_sum);
+  k_scan_tiles<<<1, 1024, 0, s>>>(tile_sum, tiles, tile_sum + tiles);
+  k_scan_add<<<(capacity + 256) / 256, 256, 0, s>>>(out, capacity, n_dev, tile_sum, tile_sum + tiles);
+}
+
+void launch_bank_bounds(const Bank &b, unsigned long long *max_bits, DeviceDiag *d, int n_sm,
+                        cudaStream_t s) {
+  cudaMemsetAsync(max_bits, 0, 2 * sizeof(unsigned long long), s);
+  k_bank_bounds<<<n_sm * 4, 256, 0, s>>>(b, d, max_bits);
+  k_set_scales<<<1, 1, 0, s>>>(d, max_bits);
+}
+
+void launch_tally_to_double(const MeshDev &m, const CellsDev &c, DeviceDiag *d, double *abs_out,
+                           double *track_out, cudaStream_t s) {
+  cudaMemsetAsync(d->sum_abs, 0, sizeof(d->sum_abs), s);
+  k_tally_to_double<<<(m.n_cells + 255) / 256, 256, 0, s>>>(m, c, d, abs_out, track_out);
+  k_tally_total<<<1, 1, 0, s>>>(d);
+}
+
+void launch_update_temperature(const MeshDev &m, const CellsDev &c, DeviceDiag *d, double dt,
+                               const double *abs_in, const double *track_in, double *mat_part,
+                               cudaStream_t s) {
+  const uint32_t blocks = (m.n_cells + 255) / 256;
+  k_update_temperature<<<blocks, 256, 0, s>>>(m, c, dt, abs_in, track_in, mat_part);
+  k_finish_temperature<<<1, 32, 0, s>>>(d, mat_part, blocks);
+}
+
+uint32_t update_temperature_parts(uint32_t n_cells) { return (n_cells + 255) / 256; }
+
+}  // namespace bgs

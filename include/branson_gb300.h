@@ -1,0 +1,199 @@
+/*
+ * branson_gb300 — C ABI of the GB300 (sm_103a) replicated-mode IMC step.
+ *
+ * One context owns one GPU stream, the replicated structured mesh, the
+ * per-cell material state, two photon banks (structure of arrays) and the
+ * per-cell tallies.  Every call returns BGS_OK (0) or an error code; the
+ * message for the last failure is bgs_last_error(ctx).  Calls on one context
+ * must come from one host thread at a time (one context per host thread, no
+ * global state).  No call falls back to the CPU: without a usable GPU
+ * bgs_create fails.
+ *
+ * Upstream interfaces each entry point replaces (file:line in Branson's src/):
+ *   bgs_set_mesh                 Mesh(...) + Mesh::initialize_physical_properties
+ *                                (mesh.h:54-127, :426-439) and GPU_Setup's
+ *                                cell upload (gpu_setup.h:23-40)
+ *   bgs_calculate_photon_energy  Mesh::calculate_photon_energy (mesh.h:237-323)
+ *   bgs_source                   make_initial_census_photons / make_photons +
+ *                                join_photon_arrays (source.h:134-366,
+ *                                census_functions.h:20-29)
+ *   bgs_transport                replicated_transport's history/event branches
+ *                                and post_process_photons
+ *                                (replicated_transport.h:33-158,
+ *                                post_process_functions.h:29-109)
+ *   bgs_update_temperature       the tally allreduce + Mesh::update_temperature
+ *                                (replicated_driver.h:90-96, mesh.h:327-423)
+ *   bgs_step                     one pass of imc_replicated_driver's loop body
+ *                                (replicated_driver.h:47-121)
+ *   bgs_replicated_transport     replicated_transport<Census_T>(...) itself
+ *                                (replicated_transport.h:33-38) with host
+ *                                photon buffers: the drop-in the C++ shim in
+ *                                branson_gb300_transport.hpp calls
+ */
+#ifndef BRANSON_GB300_H
+#define BRANSON_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define BGS_API __attribute__((visibility("default")))
+#else
+#define BGS_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum {
+  BGS_OK = 0,
+  BGS_ERR_INVALID = 1,   /* bad argument or size */
+  BGS_ERR_CUDA = 2,      /* a CUDA runtime call failed */
+  BGS_ERR_CAPACITY = 3,  /* photon bank or census buffer too small */
+  BGS_ERR_STATE = 4,     /* call made before what it needs (e.g. no mesh) */
+  BGS_ERR_DEVICE = 5,    /* a device-side check fired (see bgs_last_error) */
+  BGS_ERR_NO_DEVICE = 6  /* no CUDA device, or not an sm_103 part */
+};
+
+/* Constants::bc_type (constants.h:26) */
+enum { BGS_REFLECT = 0, BGS_VACUUM = 1, BGS_ELEMENT = 2, BGS_SOURCE = 3, BGS_PROCESSOR = 4 };
+/* Constants::event_type (constants.h:28), the photon descriptor */
+enum { BGS_EXIT = 0, BGS_PASS = 1, BGS_CENSUS = 2, BGS_SCATTER = 3, BGS_KILLED = 4, BGS_BOUND = 5 };
+/* transport algorithms (constants.h:34) */
+enum { BGS_HISTORY = 0, BGS_EVENT = 1 };
+
+typedef struct bgs_context bgs_context;
+
+/* Replicated structured mesh as the deck defines it.  Cell
+ * g = i + ngx*j + ngx*ngy*k (proto_mesh.h:106-218); its nodes are
+ * x_planes[i..i+1], y_planes[j..j+1], z_planes[k..k+1].  Regions are rows of
+ * 8 doubles: cV, rho, opacA, opacB, opacC, opacS, initial T_e, initial T_r
+ * (region.h:74-83).  bc[] is indexed X-, X+, Y-, Y+, Z-, Z+ (constants.h:27). */
+typedef struct {
+  uint32_t ngx, ngy, ngz;
+  uint32_t n_groups;                 /* BRANSON_N_GROUPS */
+  const double *x_planes, *y_planes, *z_planes;
+  const uint32_t *cell_region;       /* n_cells region indices (0-based rows) */
+  uint32_t n_regions;
+  const double *regions;             /* n_regions x 8 */
+  int32_t bc[6];
+  double T_source;
+} bgs_mesh_desc;
+
+/* Photons in host memory as structure of arrays (the Photon fields,
+ * photon.h:172-181).  The RNG of a photon is its stream number and the low
+ * counter word; the high word is the deck seed << 32 (RNG.h:318-330). */
+typedef struct {
+  double *pos_x, *pos_y, *pos_z;
+  double *dir_x, *dir_y, *dir_z;
+  double *E, *E0, *life_dx;
+  uint32_t *cell, *group;
+  uint8_t *descriptor, *source_type;
+  uint64_t *rng_stream, *rng_counter;
+} bgs_photons_host;
+
+/* Energies of one bgs_calculate_photon_energy call (mesh.h:282-322). */
+typedef struct {
+  double total_photon_E, emission_E, census_E, source_E, pre_mat_E;
+  uint64_t n_new_photons, n_initial_census;
+} bgs_energy_diag;
+
+/* What one step or transport call reports (imc_state.h:254-258 quantities). */
+typedef struct {
+  uint64_t n_transported;    /* histories in the bank this step */
+  uint64_t n_census;         /* census photons left at the end */
+  uint64_t n_segments;       /* history-loop trips (transport_photon :55) */
+  double census_E, exit_E;   /* post-process sums (post_process_functions.h:46-53) */
+  double absorbed_E, post_mat_E;
+  uint32_t device_flags;     /* nonzero: a device-side check fired */
+  uint32_t reserved;
+} bgs_transport_diag;
+
+typedef struct {
+  uint32_t step;             /* cycle number, 1-based (imc_state.h:91) */
+  uint32_t algorithm;        /* BGS_HISTORY or BGS_EVENT */
+  double dt, next_dt;        /* this step's dt and imc_state.get_next_dt() */
+} bgs_step_params;
+
+/* per-cell fields readable with bgs_get_cell_field / writable with set */
+enum {
+  BGS_FIELD_T_E = 0,         /* material temperature (cell.h:334) */
+  BGS_FIELD_T_R = 1,         /* radiation temperature from track_E (mesh.h:358) */
+  BGS_FIELD_OP_A = 2,        /* absorption opacity (cell.h:330) */
+  BGS_FIELD_OP_S = 3,        /* scattering opacity (cell.h:331) */
+  BGS_FIELD_F = 4,           /* Fleck factor (cell.h:332) */
+  BGS_FIELD_EMISSION_E = 5,  /* mesh.h:272 */
+  BGS_FIELD_CENSUS_E = 6,    /* mesh.h:274-277 */
+  BGS_FIELD_SOURCE_E = 7,    /* mesh.h:280 */
+  BGS_FIELD_ABS_E = 8,       /* last transport's absorbed-energy tally */
+  BGS_FIELD_TRACK_E = 9,     /* last transport's track-length tally */
+  BGS_FIELD_COUNT = 10
+};
+
+/* ------------------------------------------------------------ lifecycle */
+/* Create a context on `device` with room for `photon_capacity` photons per
+ * bank.  `stream` is a cudaStream_t to launch on (NULL: the context creates
+ * its own non-blocking stream).  seed and n_user_photons are the deck's
+ * <seed> and <photons> (imc_parameters.h:30-40). */
+BGS_API int bgs_create(bgs_context **ctx, int device, uint64_t photon_capacity, void *stream,
+               uint32_t seed, uint64_t n_user_photons);
+BGS_API int bgs_destroy(bgs_context *ctx);
+BGS_API const char *bgs_last_error(const bgs_context *ctx);
+BGS_API const char *bgs_status_string(int status);
+/* Library version string and the device architecture it was built for. */
+BGS_API const char *bgs_version(void);
+
+/* ---------------------------------------------------------------- mesh */
+BGS_API int bgs_set_mesh(bgs_context *ctx, const bgs_mesh_desc *mesh);
+BGS_API uint32_t bgs_n_cells(const bgs_context *ctx);
+BGS_API int bgs_get_cell_field(bgs_context *ctx, int field, double *host_out);
+BGS_API int bgs_set_cell_field(bgs_context *ctx, int field, const double *host_in);
+
+/* ------------------------------------------------------- staged step */
+BGS_API int bgs_calculate_photon_energy(bgs_context *ctx, uint32_t step, double dt, bgs_energy_diag *out);
+/* Make this step's photons on the device after the census already in the
+ * bank (step 1 also makes the initial census first). */
+BGS_API int bgs_source(bgs_context *ctx, uint32_t step, double dt);
+/* Transport every photon in the bank; census photons are compacted (in bank
+ * order, life_dx = c*next_dt) into the other bank, which becomes current. */
+BGS_API int bgs_transport(bgs_context *ctx, double next_dt, uint32_t algorithm, bgs_transport_diag *out);
+BGS_API int bgs_update_temperature(bgs_context *ctx, double dt, bgs_transport_diag *out);
+/* All four stages; `out` may be NULL (then nothing is copied back and the
+ * call does not wait for the GPU). */
+BGS_API int bgs_step(bgs_context *ctx, const bgs_step_params *p, bgs_transport_diag *out);
+/* Wait for the context's stream; returns BGS_ERR_DEVICE if a device check fired. */
+BGS_API int bgs_synchronize(bgs_context *ctx);
+
+/* --------------------------------------------------------- photon I/O */
+/* Number of photons in the current bank (the census after bgs_transport). */
+BGS_API int bgs_bank_size(bgs_context *ctx, uint64_t *n);
+/* Copy photons [offset, offset+count) of the current bank out / in. */
+BGS_API int bgs_get_photons(bgs_context *ctx, uint64_t offset, uint64_t count, const bgs_photons_host *out);
+BGS_API int bgs_set_photons(bgs_context *ctx, uint64_t count, const bgs_photons_host *in);
+
+/* ------------------------------------------------ drop-in transport */
+/* replicated_transport<Census_T> (replicated_transport.h:33-158) on host
+ * buffers: `photons` (n entries) is copied to the device, transported with
+ * the context's current cell opacities and Fleck factors, and written back
+ * in place (end states); the CENSUS photons are returned in `census` in
+ * their input order with life_dx = c*next_dt; rank_abs_E / rank_track_E
+ * (n_cells each) are overwritten with this call's tallies. */
+BGS_API int bgs_replicated_transport(bgs_context *ctx, uint64_t n, const bgs_photons_host *photons,
+                             double next_dt, uint32_t algorithm, double *rank_abs_E,
+                             double *rank_track_E, const bgs_photons_host *census,
+                             uint64_t census_capacity, uint64_t *n_census, double *census_E,
+                             double *exit_E);
+
+/* ------------------------------------------------------- instrumentation */
+/* Device time (ms) of the last transport kernel span, measured with CUDA
+ * events on the context's stream, and its launch count. */
+BGS_API int bgs_last_transport_ms(bgs_context *ctx, float *ms, uint32_t *kernel_launches);
+/* Kernels launched by this context since creation (its own kernels only). */
+BGS_API uint64_t bgs_kernel_launch_count(const bgs_context *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

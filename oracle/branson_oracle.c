@@ -31,43 +31,71 @@ static const double BO_CUTOFF = 0.01;
  * (Nrounds = 20, threefry.h:178-179). */
 static inline uint64_t rotl64(uint64_t x, unsigned r) { return (x << r) | (x >> (64u - r)); }
 
+#define BO_MIX(R)          \
+  do {                     \
+    x0 += x1;              \
+    x1 = rotl64(x1, (R));  \
+    x1 ^= x0;              \
+  } while (0)
+
+/* the 20 rounds with their rotation schedule written out, key injections
+ * 1..5 after every fourth round */
+static inline void threefry_rounds(uint64_t *p0, uint64_t *p1, const uint64_t ks[3]) {
+  uint64_t x0 = *p0 + ks[0], x1 = *p1 + ks[1];
+  BO_MIX(16); BO_MIX(42); BO_MIX(12); BO_MIX(31);
+  x0 += ks[1]; x1 += ks[2] + 1u;
+  BO_MIX(16); BO_MIX(32); BO_MIX(24); BO_MIX(21);
+  x0 += ks[2]; x1 += ks[0] + 2u;
+  BO_MIX(16); BO_MIX(42); BO_MIX(12); BO_MIX(31);
+  x0 += ks[0]; x1 += ks[1] + 3u;
+  BO_MIX(16); BO_MIX(32); BO_MIX(24); BO_MIX(21);
+  x0 += ks[1]; x1 += ks[2] + 4u;
+  BO_MIX(16); BO_MIX(42); BO_MIX(12); BO_MIX(31);
+  x0 += ks[2]; x1 += ks[0] + 5u;
+  *p0 = x0;
+  *p1 = x1;
+}
+#undef BO_MIX
+
 void bo_threefry2x64_20(const uint64_t ctr[2], const uint64_t key[2], uint64_t out[2]) {
-  static const unsigned R[8] = {16, 42, 12, 31, 16, 32, 24, 21};
   const uint64_t ks[3] = {key[0], key[1], 0x1BD11BDAA9FC1A22ULL ^ key[0] ^ key[1]};
-  uint64_t x0 = ctr[0] + ks[0];
-  uint64_t x1 = ctr[1] + ks[1];
-  for (unsigned round = 0; round < 20; ++round) {
-    x0 += x1;
-    x1 = rotl64(x1, R[round & 7u]);
-    x1 ^= x0;
-    if ((round & 3u) == 3u) {
-      const unsigned s = (round >> 2) + 1u; /* injection 1..5 */
-      x0 += ks[s % 3u];
-      x1 += ks[(s + 1u) % 3u] + s;
-    }
-  }
+  uint64_t x0 = ctr[0], x1 = ctr[1];
+  threefry_rounds(&x0, &x1, ks);
   out[0] = x0;
   out[1] = x1;
+}
+
+typedef struct {
+  uint64_t ks[3];   /* key schedule of {stream, 0} */
+  uint64_t hi;      /* counter high word: seed << 32 */
+  uint64_t counter; /* counter low word */
+} bo_rng;
+
+static inline void rng_init(bo_rng *r, uint32_t seed, uint64_t stream, uint64_t counter) {
+  r->ks[0] = stream;
+  r->ks[1] = 0;
+  r->ks[2] = 0x1BD11BDAA9FC1A22ULL ^ stream;
+  r->hi = (uint64_t)seed << 32;
+  r->counter = counter;
 }
 
 /* _ran (RNG.h:262-285): counter {data[0], data[1] = seed<<32}, key
  * {stream, 0}; the counter advances by one per draw; the first output word
  * becomes u01fixedpt<double>: ((w >> 11) | 1) * 2^-53 (RNG.h:202-238). */
-double bo_rng_draw(uint32_t seed, uint64_t stream, uint64_t *counter) {
-  const uint64_t ctr[2] = {*counter, (uint64_t)seed << 32};
-  const uint64_t key[2] = {stream, 0};
-  uint64_t out[2];
-  bo_threefry2x64_20(ctr, key, out);
-  *counter += 1; /* array.h:133-141; the high word never carries in practice */
-  return (double)((out[0] >> 11) | 1u) * (1.0 / 9007199254740992.0);
+static inline double rng_next(bo_rng *r) {
+  uint64_t x0 = r->counter, x1 = r->hi;
+  threefry_rounds(&x0, &x1, r->ks);
+  r->counter += 1; /* array.h:133-141; the high word never carries in practice */
+  return (double)((x0 >> 11) | 1u) * (1.0 / 9007199254740992.0);
 }
 
-typedef struct {
-  uint32_t seed;
-  uint64_t stream, counter;
-} bo_rng;
-
-static inline double rng_next(bo_rng *r) { return bo_rng_draw(r->seed, r->stream, &r->counter); }
+double bo_rng_draw(uint32_t seed, uint64_t stream, uint64_t *counter) {
+  bo_rng r;
+  rng_init(&r, seed, stream, *counter);
+  const double u = rng_next(&r);
+  *counter = r.counter;
+  return u;
+}
 
 /* ------------------------------------------------------------------------ */
 /* geometry */
@@ -130,8 +158,8 @@ static double face_area(const double n[6], int face) {
 }
 
 /* Cell::get_distance_to_boundary (cell.h:117-132), sgn (cell.h:23-25) */
-double bo_distance_to_boundary(const double nodes[6], const double pos[3], const double dir[3],
-                               uint32_t *surface_cross) {
+static inline double distance_to_boundary(const double nodes[6], const double pos[3],
+                                          const double dir[3], uint32_t *surface_cross) {
   double min_dist = 1.0e16;
   for (uint32_t i = 0; i < 3; i++) {
     const uint32_t index = 2 * i + (uint32_t)(0.0 < dir[i]);
@@ -142,6 +170,11 @@ double bo_distance_to_boundary(const double nodes[6], const double pos[3], const
     }
   }
   return min_dist;
+}
+
+double bo_distance_to_boundary(const double nodes[6], const double pos[3], const double dir[3],
+                               uint32_t *surface_cross) {
+  return distance_to_boundary(nodes, pos, dir, surface_cross);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -284,7 +317,8 @@ static void emission_photon(const bo_mesh *m, uint32_t g, double E, double dt, u
                             uint64_t stream, bo_photon *p) {
   double n[6];
   bo_cell_nodes(m, g, n);
-  bo_rng r = {seed, stream, 0};
+  bo_rng r;
+  rng_init(&r, seed, stream, 0);
   memset(p, 0, sizeof(*p));
   p->source_type = 2;
   uniform_position_in_cell(n, &r, p->pos);
@@ -294,7 +328,7 @@ static void emission_photon(const bo_mesh *m, uint32_t g, double E, double dt, u
   p->cell = g;
   p->life_dx = rng_next(&r) * BO_C * dt;
   p->group = (uint32_t)floor(rng_next(&r) * (double)m->n_groups);
-  p->stream = r.stream;
+  p->stream = stream;
   p->counter = r.counter;
   p->descriptor = BO_PASS;
 }
@@ -304,7 +338,8 @@ static void boundary_source_photon(const bo_mesh *m, uint32_t g, double E, doubl
                                    uint32_t seed, uint64_t stream, int face, bo_photon *p) {
   double n[6];
   bo_cell_nodes(m, g, n);
-  bo_rng r = {seed, stream, 0};
+  bo_rng r;
+  rng_init(&r, seed, stream, 0);
   memset(p, 0, sizeof(*p));
   p->source_type = 1;
   uniform_position_on_face(n, &r, face, p->pos);
@@ -314,7 +349,7 @@ static void boundary_source_photon(const bo_mesh *m, uint32_t g, double E, doubl
   p->cell = g;
   p->life_dx = rng_next(&r) * BO_C * dt;
   p->group = (uint32_t)floor(rng_next(&r) * (double)m->n_groups);
-  p->stream = r.stream;
+  p->stream = stream;
   p->counter = r.counter;
   p->descriptor = BO_PASS;
 }
@@ -324,7 +359,8 @@ static void initial_census_photon(const bo_mesh *m, uint32_t g, double E, double
                                   uint32_t seed, uint64_t stream, bo_photon *p) {
   double n[6];
   bo_cell_nodes(m, g, n);
-  bo_rng r = {seed, stream, 0};
+  bo_rng r;
+  rng_init(&r, seed, stream, 0);
   memset(p, 0, sizeof(*p));
   p->source_type = 0;
   uniform_position_in_cell(n, &r, p->pos);
@@ -334,7 +370,7 @@ static void initial_census_photon(const bo_mesh *m, uint32_t g, double E, double
   p->cell = g;
   p->life_dx = BO_C * dt;
   p->group = (uint32_t)floor(rng_next(&r) * (double)m->n_groups);
-  p->stream = r.stream;
+  p->stream = stream;
   p->counter = r.counter;
   p->descriptor = BO_PASS;
 }
@@ -400,14 +436,19 @@ static uint32_t sample_emission_group(bo_rng *r, double op_a, uint32_t n_groups)
   return (uint32_t)new_group;
 }
 
-/* transport_photon, AoS form (history_based_transport.h:33-141). */
+/* transport_photon, AoS form (history_based_transport.h:33-141).  The cell
+ * is tracked by its (i, j, k) position so that nodes, neighbours and
+ * boundary codes come from the plane arrays without any division, the way
+ * the upstream loop reads them from its precomputed Cell. */
 static uint64_t transport_photon(const bo_mesh *m, const bo_cells *c, uint32_t seed, bo_photon *p,
                                  double *abs_t, double *track_t) {
-  bo_rng r = {seed, p->stream, p->counter};
+  bo_rng r;
+  rng_init(&r, seed, p->stream, p->counter);
   uint32_t surface_cross = 0;
   uint32_t cell = p->cell;
-  double nodes[6];
-  bo_cell_nodes(m, cell, nodes);
+  const uint32_t sxy = m->ngx * m->ngy;
+  uint32_t ci = cell % m->ngx, cj = (cell / m->ngx) % m->ngy, ck = cell / sxy;
+  double nodes[6] = {m->x[ci], m->x[ci + 1], m->y[cj], m->y[cj + 1], m->z[ck], m->z[ck + 1]};
   double thread_abs = 0.0, thread_track = 0.0;
   uint64_t segments = 0;
   int active = 1;
@@ -419,7 +460,7 @@ static uint64_t transport_photon(const bo_mesh *m, const bo_cells *c, uint32_t s
     const double total_sigma_s = (1.0 - f) * sigma_a + sigma_s;
     const double dist_to_scatter =
         (total_sigma_s > 0.0) ? -log(rng_next(&r)) / total_sigma_s : 1.0e100;
-    const double dist_to_boundary = bo_distance_to_boundary(nodes, p->pos, p->dir, &surface_cross);
+    const double dist_to_boundary = distance_to_boundary(nodes, p->pos, p->dir, &surface_cross);
     const double dist_to_census = p->life_dx;
     /* std::min(a, b) is (b < a) ? b : a */
     const double db_dc = (dist_to_census < dist_to_boundary) ? dist_to_census : dist_to_boundary;
@@ -444,23 +485,36 @@ static uint64_t transport_photon(const bo_mesh *m, const bo_cells *c, uint32_t s
         p->group = sample_emission_group(&r, sigma_a, m->n_groups);
       p->descriptor = BO_SCATTER;
     } else if (dist_to_event == dist_to_boundary) {
-      uint32_t next;
-      const int bc = cell_bc(m, cell, surface_cross, &next);
+      /* interior faces are ELEMENT, domain faces carry the deck's boundary
+       * (proto_mesh.h:156-202) */
+      int interior;
+      switch (surface_cross) {
+      case 0: interior = ci > 0; break;
+      case 1: interior = ci + 1 < m->ngx; break;
+      case 2: interior = cj > 0; break;
+      case 3: interior = cj + 1 < m->ngy; break;
+      case 4: interior = ck > 0; break;
+      default: interior = ck + 1 < m->ngz; break;
+      }
+      const int bc = interior ? BO_ELEMENT : m->bc[surface_cross];
       if (bc == BO_ELEMENT) {
         abs_t[cell] += thread_abs;
         track_t[cell] += thread_track;
-        p->cell = next;
-        cell = next;
-        bo_cell_nodes(m, cell, nodes);
+        switch (surface_cross) {
+        case 0: --ci; cell -= 1; break;
+        case 1: ++ci; cell += 1; break;
+        case 2: --cj; cell -= m->ngx; break;
+        case 3: ++cj; cell += m->ngx; break;
+        case 4: --ck; cell -= sxy; break;
+        default: ++ck; cell += sxy; break;
+        }
+        p->cell = cell;
+        nodes[0] = m->x[ci]; nodes[1] = m->x[ci + 1];
+        nodes[2] = m->y[cj]; nodes[3] = m->y[cj + 1];
+        nodes[4] = m->z[ck]; nodes[5] = m->z[ck + 1];
         p->descriptor = BO_BOUND;
         thread_abs = 0.0;
         thread_track = 0.0;
-      } else if (bc == BO_PROCESSOR) {
-        active = 0;
-        p->cell = next;
-        p->descriptor = BO_PASS;
-        abs_t[cell] += thread_abs;
-        track_t[cell] += thread_track;
       } else if (bc == BO_VACUUM || bc == BO_SOURCE) {
         active = 0;
         p->descriptor = BO_EXIT;

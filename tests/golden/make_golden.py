@@ -1,0 +1,56 @@
+"""Generate the golden vectors in tests/golden/ from the upstream code.
+
+Runs oracle/_ref/ref_harness_g{1,30} -- the upstream Branson headers compiled
+unmodified from the reference checkout (make -C oracle ref) -- on three
+small synthetic decks and stores, per time step, the photon list before
+transport, the end states and census after transport, and the per-cell
+energies, tallies and temperatures, as compressed .npz files.
+
+    python tests/golden/make_golden.py        # needs the reference checkout
+
+The decks are generated by branson_gb300.deck, so the fixtures are
+self-describing: each .npz also holds the deck XML it was made from.
+"""
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from branson_gb300 import deck as D  # noqa: E402
+import oracle as O  # noqa: E402
+
+CASES = {
+    "marshak_g1": (lambda: D.marshak_wave(n_cells=40, photons=1500, n_steps=2), 2),
+    "hot_zone_g1": (lambda: D.hot_zone(n_per_axis=5, photons=1500, n_steps=2), 2),
+    "hohlraum_g30": (lambda: D.hohlraum(n_per_axis=8, photons=1500, n_steps=2, n_groups=30), 2),
+}
+
+
+def main():
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
+    for name, (mk, steps) in CASES.items():
+        dk = mk()
+        with tempfile.TemporaryDirectory() as tmp:
+            O.run_reference_harness(dk, tmp, steps, n_threads=1)
+            out = {"deck_xml": np.array(dk.to_xml()), "n_groups": np.array(dk.n_groups),
+                   "n_steps": np.array(steps)}
+            for s in range(1, steps + 1):
+                h = O.read_harness_step(tmp, s, dk.n_cells)
+                for k in ("source", "end", "census", "cells"):
+                    out[f"s{s}_{k}"] = h[k]
+                out[f"s{s}_scalars_keys"] = np.array(sorted(h["scalars"]))
+                out[f"s{s}_scalars"] = np.array([h["scalars"][k] for k in sorted(h["scalars"])])
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **out)
+        print(f"{path}: {os.path.getsize(path)} bytes")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,163 @@
+"""GPU path vs the oracle (the C restatement pinned to the upstream code).
+
+Two forms, both through the C ABI:
+  * drop-in: the oracle makes a step's photon list; bgs_replicated_transport
+    transports exactly those photons on host buffers; end states, census
+    (order and values), tallies and post-process sums are compared;
+  * device-resident staged step: energies, photon counts and the sourced
+    photons (matched by RNG stream), tallies and the temperature update.
+"""
+import numpy as np
+import pytest
+
+from parity import CELL_RTOL, END_RTOL, bitwise_fraction, by_stream, close, compare_photons
+
+pytestmark = pytest.mark.gpu
+
+C_LIGHT = 299.792458
+
+
+def _decks():
+    from branson_gb300 import deck as D
+    return {
+        "marshak": D.marshak_wave(n_cells=100, photons=20000, n_steps=3),
+        "hot_zone": D.hot_zone(n_per_axis=10, photons=20000, n_steps=3),
+        "hohlraum30": D.hohlraum(n_per_axis=10, photons=20000, n_steps=2, n_groups=30),
+    }
+
+
+def _extent(dk):
+    x, y, z = dk.planes()
+    return max(x[-1] - x[0], y[-1] - y[0], z[-1] - z[0], C_LIGHT * dk.dt_start)
+
+
+@pytest.mark.parametrize("name", ["marshak", "hot_zone", "hohlraum30"])
+def test_dropin_transport_matches_oracle(gpu_lib, name):
+    import oracle as O
+    from branson_gb300.engine import ReplicatedIMC, arrays_to_records, records_to_arrays
+
+    dk = _decks()[name]
+    orc = O.Oracle(dk)
+    gpu = ReplicatedIMC(dk)
+    ext = _extent(dk)
+    try:
+        for _ in range(2):
+            step = orc.step_no
+            en, photons = orc.source(step)
+            nd = orc.next_dt()
+            for f in ("op_a", "op_s", "f"):
+                gpu.set_field(f, orc.arr[f])
+            ph = records_to_arrays(photons)
+            abs_g, trk_g, census_g, ce_g, ex_g = gpu.replicated_transport(ph, nd)
+            end_g = arrays_to_records(ph, O.PHOTON_DTYPE)
+            abs_o, trk_o, census_o, ce_o, ex_o, segs, _ = orc.transport(photons, nd)
+            compare_photons(end_g, photons, ext, f"{name} step {step} end states")
+            print(f"{name} step {step}: {len(photons)} histories, "
+                  f"{100 * bitwise_fraction(end_g, photons):.2f}% bit-identical end states")
+            compare_photons(arrays_to_records(census_g, O.PHOTON_DTYPE), census_o, ext,
+                            f"{name} step {step} census")
+            close(abs_g, abs_o, CELL_RTOL, 0.0, f"{name} abs_E")
+            close(trk_g, trk_o, CELL_RTOL, 0.0, f"{name} track_E")
+            close([ce_g, ex_g], [ce_o, ex_o], CELL_RTOL, 1e-300, f"{name} census/exit E")
+            # advance the oracle exactly as its driver does
+            import ctypes as C
+            ta, pm = C.c_double(), C.c_double()
+            O.lib().bo_update_temperature(C.byref(orc.mesh), C.byref(orc.cells), orc.dt,
+                                          O._dptr(abs_o), O._dptr(trk_o), C.byref(ta), C.byref(pm))
+            orc.census = census_o
+            orc.time += orc.dt
+            orc.dt = nd
+            orc.step_no += 1
+    finally:
+        gpu.close()
+
+
+@pytest.mark.parametrize("name", ["marshak", "hot_zone", "hohlraum30"])
+def test_device_step_matches_oracle(gpu_lib, name):
+    import oracle as O
+    from branson_gb300.engine import ReplicatedIMC, arrays_to_records
+
+    dk = _decks()[name]
+    orc = O.Oracle(dk)
+    gpu = ReplicatedIMC(dk)
+    ext = _extent(dk)
+    try:
+        for _ in range(2):
+            step = orc.step_no
+            # keep the material state identical so each step is compared on its own
+            gpu.set_field("T_e", orc.arr["T_e"])
+            census_in = gpu.bank_size() if step > 1 else 0
+            e = gpu.calculate_photon_energy(step, gpu.dt)
+            res = orc.step()
+            for fname, ref in (("op_a", res.op_a), ("f", res.f), ("emission_E", res.emission_cell_E),
+                               ("census_E", res.census_cell_E), ("source_E", res.source_cell_E)):
+                close(gpu.get_field(fname), ref, 1e-13, 0.0, f"{name} step {step} {fname}")
+            close([e["total_photon_E"], e["pre_mat_E"]], [res.total_photon_E, res.pre_mat_E], 1e-13, 0.0,
+                  "totals")
+            is_new = res.source["stream"] >= 10000000000000 * step
+            assert e["n_new_photons"] == int(is_new.sum())
+            gpu.source(step, gpu.dt)
+            bank = arrays_to_records(gpu.photons(), O.PHOTON_DTYPE)
+            # photons made this step, matched to the oracle by RNG stream
+            new_g = by_stream(bank[census_in:])
+            new_o = by_stream(res.source[is_new]) if step > 1 else by_stream(res.source)
+            compare_photons(new_g, new_o, ext, f"{name} step {step} source", check_desc=False)
+            t = gpu.transport(res.next_dt)
+            assert t["device_flags"] == 0
+            assert t["n_transported"] == len(res.source)
+            assert t["n_census"] == len(res.census)
+            close(gpu.get_field("abs_E"), res.abs_E, CELL_RTOL, 0.0, f"{name} step {step} abs_E")
+            close(gpu.get_field("track_E"), res.track_E, CELL_RTOL, 0.0, f"{name} step {step} track_E")
+            close([t["census_E"], t["exit_E"]], [res.census_E, res.exit_E], CELL_RTOL, 1e-300, "census/exit")
+            u = gpu.update_temperature(gpu.dt)
+            close(gpu.get_field("T_e"), res.T_e, CELL_RTOL, 0.0, f"{name} step {step} T_e")
+            close(gpu.get_field("T_r"), res.T_r, CELL_RTOL, 0.0, f"{name} step {step} T_r")
+            close([u["absorbed_E"], u["post_mat_E"]], [res.absorbed_E, res.post_mat_E], CELL_RTOL, 0.0,
+                  "absorbed/post_mat")
+            census_g = by_stream(arrays_to_records(gpu.photons(), O.PHOTON_DTYPE))
+            compare_photons(census_g, by_stream(res.census), ext, f"{name} step {step} census")
+            gpu.advance_time(res.next_dt)
+    finally:
+        gpu.close()
+
+
+@pytest.mark.parametrize("name", ["marshak_g1", "hot_zone_g1", "hohlraum_g30"])
+def test_gpu_against_upstream_golden(gpu_lib, name):
+    """The GPU drop-in transport on the upstream photon lists (golden vectors
+    written by the upstream headers) reproduces the upstream end states,
+    census and tallies; the device source reproduces the upstream photons."""
+    import os
+    import oracle as O
+    from branson_gb300 import deck as D
+    from branson_gb300.engine import ReplicatedIMC, arrays_to_records, records_to_arrays
+
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", f"{name}.npz"))
+    dk = D.parse_xml(str(g["deck_xml"]), n_groups=int(g["n_groups"]))
+    ext = _extent(dk)
+    with ReplicatedIMC(dk) as gpu:
+        T_e = None
+        for s in range(1, int(g["n_steps"]) + 1):
+            cells = g[f"s{s}_cells"]
+            if T_e is not None:
+                gpu.set_field("T_e", T_e)
+            gpu.calculate_photon_energy(s, gpu.dt)
+            close(gpu.get_field("op_a"), cells[:, 0], 1e-13, 0.0, f"{name} s{s} op_a")
+            close(gpu.get_field("emission_E"), cells[:, 2], 1e-13, 0.0, f"{name} s{s} emission_E")
+            src = g[f"s{s}_source"]
+            if s == 1:
+                gpu.source(1, gpu.dt)
+                made = by_stream(arrays_to_records(gpu.photons(), O.PHOTON_DTYPE))
+                compare_photons(made, by_stream(src), ext, f"{name} s1 sourced", check_desc=False)
+            gpu.set_field("op_a", cells[:, 0])
+            gpu.set_field("f", cells[:, 1])
+            gpu.set_field("op_s", np.zeros(dk.n_cells))
+            ph = records_to_arrays(src)
+            nd = dk.dt_start
+            abs_g, trk_g, census_g, _, _ = gpu.replicated_transport(ph, nd)
+            compare_photons(arrays_to_records(ph, O.PHOTON_DTYPE), g[f"s{s}_end"], ext, f"{name} s{s} end")
+            compare_photons(arrays_to_records(census_g, O.PHOTON_DTYPE), g[f"s{s}_census"], ext,
+                            f"{name} s{s} census")
+            close(abs_g, cells[:, 5], CELL_RTOL, 0.0, f"{name} s{s} abs_E")
+            close(trk_g, cells[:, 6], CELL_RTOL, 0.0, f"{name} s{s} track_E")
+            T_e = cells[:, 7]
+            gpu.advance_time(nd)
