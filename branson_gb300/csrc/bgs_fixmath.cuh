@@ -1,0 +1,464 @@
+// Integer fixed-point evaluation of the transcendental functions on the
+// transport hot path, rounded once to IEEE double.
+//
+// GB300 executes FP64 at 2 lanes/clock/SM, while 32-bit integer arithmetic
+// issues at up to 64 lanes/clock/SM.  These functions evaluate log and exp
+// with ~62-63 significant bits using only 64/128-bit integer arithmetic and
+// round the result to nearest, so they take the integer pipes instead of
+// the FP64 pipe, and their results are the correctly rounded doubles except
+// when the exact value lies within about 2^-9 ulp of a rounding midpoint.
+//
+// Methods (published, restated here in fixed point):
+//   log: P. T. P. Tang, "Table-driven implementation of the logarithm
+//        function in IEEE floating-point arithmetic", ACM TOMS 16(4), 1990:
+//        x = F_j (1 + r) with F_j = 1 + j/1024, ln(1+r) by its Taylor series;
+//        near u = 1 the series of -ln(1 - v) in the exact v = 1 - u.
+//   exp: P. T. P. Tang, "Table-driven implementation of the exponential
+//        function in IEEE floating-point arithmetic", ACM TOMS 15(2), 1989:
+//        tau = (32*q + j) ln2/1024 + s, exp(-tau) = 2^-q 2^(-j/1024) e^(-s),
+//        e^(-s) by its Taylor series.
+//   sin/cos: Cody-Waite style reduction by pi/2 with a 128-bit 2/pi, octant
+//        symmetry, Taylor series on [0, pi/4].
+// Tables (bgs_fixmath_tables.h) are generated from Python's decimal module.
+// The same source compiles for the host (tests compare it against quad
+// precision and glibc) and for the device.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+#include "bgs_fixmath_tables.h"
+
+#if defined(__CUDACC__)
+#define BGS_HD __host__ __device__ __forceinline__
+#else
+#define BGS_HD inline
+#endif
+
+namespace bgs {
+namespace fix {
+
+typedef unsigned __int128 u128;
+
+#if defined(__CUDACC__)
+__device__ const uint64_t d_log_invf[fixtab::kBins] = {BGS_LOG_INVF_INIT};
+__device__ const uint64_t d_log_lnf[2 * fixtab::kBins] = {BGS_LOG_LNF_INIT};
+__device__ const uint64_t d_exp2_neg[fixtab::kBins] = {BGS_EXP2_NEG_INIT};
+#endif
+static const uint64_t h_log_invf[fixtab::kBins] = {BGS_LOG_INVF_INIT};
+static const uint64_t h_log_lnf[2 * fixtab::kBins] = {BGS_LOG_LNF_INIT};
+static const uint64_t h_exp2_neg[fixtab::kBins] = {BGS_EXP2_NEG_INIT};
+
+BGS_HD uint64_t log_invf(uint32_t j) {
+#if defined(__CUDA_ARCH__)
+  return __ldg(&d_log_invf[j]);
+#else
+  return h_log_invf[j];
+#endif
+}
+BGS_HD u128 log_lnf(uint32_t j) {
+#if defined(__CUDA_ARCH__)
+  const uint64_t hi = __ldg(&d_log_lnf[2 * j]), lo = __ldg(&d_log_lnf[2 * j + 1]);
+#else
+  const uint64_t hi = h_log_lnf[2 * j], lo = h_log_lnf[2 * j + 1];
+#endif
+  return ((u128)hi << 64) | lo;
+}
+BGS_HD uint64_t exp2_neg(uint32_t j) {
+#if defined(__CUDA_ARCH__)
+  return __ldg(&d_exp2_neg[j]);
+#else
+  return h_exp2_neg[j];
+#endif
+}
+
+BGS_HD uint64_t mulhi(uint64_t a, uint64_t b) {
+#if defined(__CUDA_ARCH__)
+  return __umul64hi(a, b);
+#else
+  return (uint64_t)(((u128)a * b) >> 64);
+#endif
+}
+
+BGS_HD int clz64(uint64_t x) {
+#if defined(__CUDA_ARCH__)
+  return __clzll((long long)x);
+#else
+  return x ? __builtin_clzll(x) : 64;
+#endif
+}
+
+BGS_HD double bits_to_double(uint64_t b) {
+#if defined(__CUDA_ARCH__)
+  return __longlong_as_double((long long)b);
+#else
+  double d;
+  std::memcpy(&d, &b, sizeof d);
+  return d;
+#endif
+}
+
+BGS_HD uint64_t double_to_bits(double d) {
+#if defined(__CUDA_ARCH__)
+  return (uint64_t)__double_as_longlong(d);
+#else
+  uint64_t b;
+  std::memcpy(&b, &d, sizeof b);
+  return b;
+#endif
+}
+
+// Round the positive value W * 2^-scale (W != 0) to the nearest double.
+// Values below the normal range flush to zero (callers never produce them
+// on the paths that use this).
+BGS_HD double round_u128(u128 W, int scale) {
+  const uint64_t hi = (uint64_t)(W >> 64), lo = (uint64_t)W;
+  const int p = hi ? 127 - clz64(hi) : 63 - clz64(lo);  // top set bit
+  uint64_t mant;
+  bool up;
+  if (p >= 53) {
+    const int sh = p - 52;  // bits dropped
+    mant = (uint64_t)(W >> sh);
+    const u128 rem = W & (((u128)1 << sh) - 1);
+    const u128 half = (u128)1 << (sh - 1);
+    up = rem > half || (rem == half && (mant & 1));
+  } else {
+    mant = (uint64_t)(W << (52 - p));
+    up = false;
+  }
+  int e2 = p - scale;  // value = mant * 2^(e2 - 52)
+  if (up) {
+    ++mant;
+    if (mant >> 53) { mant >>= 1; ++e2; }
+  }
+  const int be = e2 + 1023;
+  if (be <= 0) return 0.0;
+  return bits_to_double(((uint64_t)be << 52) | (mant & 0x000FFFFFFFFFFFFFULL));
+}
+
+// -ln(u) for the RNG draw u = m * 2^-53 (u01fixedpt: m odd, 1 <= m < 2^53).
+// The result is the value -log(u) rounds to (the upstream distance to
+// collision numerator, history_based_transport.h:62-63).
+BGS_HD double neg_log_u53(uint64_t m) {
+  const uint64_t n = (1ULL << 53) - m;  // v = 1 - u = n * 2^-53, exact
+  if (n < (1ULL << 42)) {
+    // v < 2^-11: -ln(1-v) = v (1 + v/2 + v^2/3 + v^3/4 + v^4/5 + v^5/6), V = v*2^64
+    const uint64_t V = n << 11;
+    uint64_t t = 0x2AAAAAAAAAAAAAABULL;           // 1/6
+    t = 0x3333333333333333ULL + mulhi(V, t);       // 1/5
+    t = 0x4000000000000000ULL + mulhi(V, t);       // 1/4
+    t = 0x5555555555555555ULL + mulhi(V, t);       // 1/3
+    t = 0x8000000000000000ULL + mulhi(V, t);       // 1/2
+    const uint64_t T = mulhi(V, t);                // (S - 1) * 2^64
+    const u128 L = ((u128)V << 64) + (u128)V * T;  // L * 2^128
+    return round_u128(L, 128);
+  }
+  const int e = 63 - clz64(m);                     // m in [2^e, 2^(e+1))
+  const uint64_t k = 53 - e;                       // u = x 2^-k, x in [1, 2)
+  const uint64_t X = m << (63 - e);                // x * 2^63
+  const uint32_t j = (uint32_t)(X >> 53) & 1023u;  // F_j = 1 + j/1024
+  const uint64_t f = X & ((1ULL << 53) - 1);       // (x - F_j) * 2^63
+  // R = r * 2^74 with r = (x - F_j)/F_j < 2^-10
+  const uint64_t R = j ? mulhi(f << 11, log_invf(j)) : (f << 11);
+  // ln(1+r) = r - r^2 (1/2 - r(1/3 - r(1/4 - r(1/5 - r(1/6 - r/7)))))
+  uint64_t b = 0x2AAAAAAAAAAAAAABULL - (mulhi(R, 0x2492492492492492ULL) >> 10);  // 1/6 - r/7
+  b = 0x3333333333333333ULL - (mulhi(R, b) >> 10);                                // 1/5 - ...
+  b = 0x4000000000000000ULL - (mulhi(R, b) >> 10);                                // 1/4 - ...
+  b = 0x5555555555555555ULL - (mulhi(R, b) >> 10);                                // 1/3 - ...
+  b = 0x8000000000000000ULL - (mulhi(R, b) >> 10);                                // 1/2 - ...
+  const uint64_t R2 = (uint64_t)(((u128)R * R) >> 64);                           // r^2 * 2^84
+  const uint64_t Q = mulhi(R2, b);                                                // r^2 b * 2^84
+  // L = k ln2 - ln F_j - r + r^2 b, scaled by 2^120
+  const u128 ln2 = ((u128)fixtab::kLn2_120_hi << 64) | fixtab::kLn2_120_lo;
+  u128 W = ln2 * k;
+  W -= log_lnf(j);
+  W -= (u128)R << 46;
+  W += (u128)Q << 36;
+  return round_u128(W, 120);
+}
+
+// exp(-tau) for tau >= 0: the factor exp(-sigma_a*f*d) of the implicit-capture
+// weight decay (history_based_transport.h:74).  tau above 700 (result below
+// 1e-304) returns the CUDA/libm value instead of the fixed-point path.
+BGS_HD double exp_neg(double tau) {
+  const uint64_t tb = double_to_bits(tau);
+  const int te = (int)((tb >> 52) & 0x7FF);
+  if (te == 0) return 1.0;  // tau = 0 (or subnormal: exp rounds to 1)
+  if (!(tau <= 700.0)) return tau == tau ? exp(-tau) : tau;
+  // T = tau * 2^96 as a 128-bit integer (truncating below 2^-96)
+  const uint64_t tm = (tb & 0x000FFFFFFFFFFFFFULL) | 0x0010000000000000ULL;
+  const int sh = te - 1075 + 96;  // tau = tm * 2^(te-1075)
+  u128 T;
+  if (sh >= 0) T = (u128)tm << sh;
+  else T = sh > -64 ? (u128)(tm >> (-sh)) : (u128)0;
+  // N ~ floor(tau * 1024/ln2) from the top bits, then corrected exactly
+  const uint64_t A = (uint64_t)(T >> 44);  // tau * 2^52
+  uint64_t N = mulhi(A, fixtab::kInvLn2_1024_q12);
+  const u128 L = ((u128)fixtab::kLn2_1024_96_hi << 64) | fixtab::kLn2_1024_96_lo;
+  u128 NL = L * N;
+  for (int it = 0; it < 4 && NL > T; ++it) { --N; NL -= L; }
+  u128 S = T - NL;
+  for (int it = 0; it < 4 && S >= L; ++it) { ++N; S -= L; }
+  // s * 2^73 (s < ln2/1024 < 2^-10.5)
+  const uint64_t s73 = (uint64_t)(S >> 23);
+  // e^-s = 1 - s (1 - s (1/2 - s (1/6 - s (1/24 - s/120))))
+  uint64_t b = 0x0AAAAAAAAAAAAAABULL - (mulhi(s73, 0x0222222222222222ULL) >> 9);  // 1/24 - s/120
+  b = 0x2AAAAAAAAAAAAAABULL - (mulhi(s73, b) >> 9);                                // 1/6 - ...
+  b = 0x8000000000000000ULL - (mulhi(s73, b) >> 9);                                // 1/2 - ...
+  b = (uint64_t)0 - (mulhi(s73, b) >> 9);                                          // 1 - s(...) (mod 2^64)
+  // P = 1 - s*b: b represents 1 - small (b == 0 means exactly 1)
+  const uint64_t sb = b ? (mulhi(s73, b) >> 9) : (s73 >> 9);
+  const uint32_t j = (uint32_t)(N & 1023u);
+  const uint64_t q = N >> 10;
+  const uint64_t E = exp2_neg(j);  // 2^(63 - j/1024)
+  u128 W;
+  if (sb == 0) {
+    W = (u128)E << 64;
+  } else {
+    const uint64_t P = (uint64_t)0 - sb;  // (1 - s b) * 2^64
+    W = (u128)E * P;
+  }
+  return round_u128(W, 127 + (int)q);
+}
+
+
+// sin and cos of 0 < phi < 8, the scattering azimuth phi = 2 pi u
+// (get_uniform_angle, sampling_functions.h:63-67).  phi * 2/pi is formed
+// exactly enough in Q124 (128-bit constant), the quadrant and octant are
+// taken off by symmetry, and sin/cos of the remaining angle in [0, pi/4] are
+// Taylor polynomials in fixed point; the small one of the pair is always a
+// sine computed relative to its argument, so tiny results keep full
+// precision.  Results are rounded to nearest.
+BGS_HD double round_u64_scaled(uint64_t mant_hi, uint64_t mant_lo, int scale) {
+  return round_u128(((u128)mant_hi << 64) | mant_lo, scale);
+}
+
+BGS_HD void sincos_phi(double phi, double *s_out, double *c_out) {
+  constexpr uint64_t kS[10] = {BGS_SIN_COEF_INIT};
+  constexpr uint64_t kCo[10] = {BGS_COS_COEF_INIT};
+  const uint64_t pb = double_to_bits(phi);
+  const int be = (int)((pb >> 52) & 0x7FF);
+  if (be == 0 || !(phi < 8.0) || !(phi > 0.0)) {
+#if defined(__CUDA_ARCH__)
+    sincos(phi, s_out, c_out);
+#else
+    *s_out = std::sin(phi);
+    *c_out = std::cos(phi);
+#endif
+    return;
+  }
+  const int e = be - 1023;  // phi = M * 2^(e - 52), e <= 2
+  const uint64_t M = (pb & 0x000FFFFFFFFFFFFFULL) | 0x0010000000000000ULL;
+  // M * (2/pi * 2^128) as three words w2:w1:w0
+  const u128 plo = (u128)M * fixtab::kTwoOverPi_128_lo;
+  const u128 phi_ = (u128)M * fixtab::kTwoOverPi_128_hi;
+  const uint64_t w0 = (uint64_t)plo;
+  const u128 mid = (plo >> 64) + (uint64_t)phi_;
+  const uint64_t w1 = (uint64_t)mid;
+  const uint64_t w2 = (uint64_t)(phi_ >> 64) + (uint64_t)(mid >> 64);
+  // Y = phi * 2/pi * 2^124 = (w2:w1:w0) >> (56 - e)
+  const int sh = 56 - e;  // 54 .. 107 for the phi this is called with
+  u128 Y;
+  if (sh < 64) {
+    Y = ((u128)w2 << (128 - sh)) | ((((u128)w1 << 64) | w0) >> sh);
+  } else if (sh < 128) {
+    Y = (((u128)w2 << 64) | w1) >> (sh - 64);
+  } else {
+    Y = (u128)(w2 >> (sh - 128));
+  }
+  (void)w0;
+  const unsigned quad = (unsigned)(Y >> 124) & 3u;
+  const u128 mask = (((u128)1) << 124) - 1;
+  u128 t = Y & mask;
+  const u128 half = ((u128)1) << 123;
+  const bool swap = t > half;
+  const u128 x = swap ? ((((u128)1) << 124) - t) : t;  // x in (0, 1/2], Q124
+  double sv, cv;  // sin and cos of x*pi/2
+  if (x == 0) {
+    sv = 0.0;
+    cv = 1.0;
+  } else {
+    const uint64_t xh = (uint64_t)(x >> 64), xl = (uint64_t)x;
+    const int lz = xh ? clz64(xh) : 64 + clz64(xl);
+    const u128 xn = x << lz;
+    const uint64_t Xn = (uint64_t)(xn >> 64);               // x = Xn * 2^(-60-lz)
+    const uint64_t Tm = mulhi(Xn, fixtab::kPiOver2_q62);     // theta = Tm * 2^(-58-lz)
+    const uint64_t th64 = lz >= 6 ? (lz - 6 >= 64 ? 0 : Tm >> (lz - 6)) : Tm << (6 - lz);  // theta * 2^64
+    const uint64_t y = mulhi(th64, th64);                    // theta^2 * 2^64
+    uint64_t b = kS[9];
+#pragma unroll
+    for (int k = 8; k >= 0; --k) b = kS[k] - mulhi(y, b);   // 1/3! - y(1/5! - ...)
+    const uint64_t sb = mulhi(y, b);                          // y * b
+    const u128 Ws = sb ? (u128)Tm * ((uint64_t)0 - sb) : ((u128)Tm << 64);
+    sv = round_u128(Ws, 122 + lz);
+    uint64_t c = kCo[9];
+#pragma unroll
+    for (int k = 8; k >= 0; --k) c = kCo[k] - mulhi(y, c);  // 1/2! - y(1/4! - ...)
+    const uint64_t cb = mulhi(y, c);
+    cv = cb ? round_u128((u128)((uint64_t)0 - cb), 64) : 1.0;
+  }
+  const double so = swap ? cv : sv;  // sin, cos of (t*pi/2)
+  const double co = swap ? sv : cv;
+  switch (quad) {
+    case 0: *s_out = so; *c_out = co; break;
+    case 1: *s_out = co; *c_out = -so; break;
+    case 2: *s_out = -so; *c_out = -co; break;
+    default: *s_out = -co; *c_out = so; break;
+  }
+}
+
+
+// ------------------------------------------------------------------------
+// Correctly rounded division and square root in integer arithmetic.  These
+// reproduce IEEE-754 round-to-nearest-even results exactly (they are checked
+// bit for bit against the hardware FP64 operations) for positive normal
+// operands and normal results; anything else goes to the FP64 operation.
+
+// floor(f * 2^shift) for a positive normal float, from its bits, saturating
+// at 2^64 - 1 (no floating-point conversion instruction needed)
+BGS_HD uint64_t float_to_fixed(float f, int shift) {
+  uint32_t b;
+#if defined(__CUDA_ARCH__)
+  b = __float_as_uint(f);
+#else
+  std::memcpy(&b, &f, sizeof b);
+#endif
+  const int e = (int)((b >> 23) & 0xFF) - 150 + shift;  // f = m * 2^(exp-150)
+  const uint64_t m = (b & 0x7FFFFFu) | 0x800000u;
+  if (e > 40) return ~0ULL;
+  if (e >= 0) return m << e;
+  return e > -64 ? m >> (-e) : 0ULL;
+}
+
+BGS_HD float u64_to_float_approx(uint64_t x) {  // x < 2^24, exact
+#if defined(__CUDA_ARCH__)
+  return __uint2float_rn((unsigned)x);
+#else
+  return (float)x;
+#endif
+}
+
+// floor(2^116 / M) for a 53-bit mantissa M in (2^52, 2^53): a 64-bit
+// reciprocal, from a float seed refined by two Newton steps in fixed point
+// and corrected to the exact floor.
+BGS_HD uint64_t recip116(uint64_t M) {
+  const float mf = u64_to_float_approx(M >> 29);  // M / 2^29, 24 bits
+#if defined(__CUDA_ARCH__)
+  const float rf = __frcp_rn(mf);
+#else
+  const float rf = 1.0f / mf;
+#endif
+  uint64_t r = float_to_fixed(rf, 87);  // ~2^116/M
+  // Newton: r <- r (2 - M r / 2^116) in fixed point, twice
+  for (int it = 0; it < 2; ++it) {
+    const u128 mr = (u128)M * r;
+    const u128 err = (((u128)1) << 117) - mr;  // (2 - M r/2^116) * 2^116
+    r = (uint64_t)(((u128)r * (uint64_t)(err >> 53)) >> 63);
+  }
+  // exact correction to floor(2^116/M)
+  const u128 P = ((u128)1) << 116;
+  u128 mr = (u128)M * r;
+  for (int it = 0; it < 8 && mr > P; ++it) { --r; mr -= M; }
+  for (int it = 0; it < 8 && P - mr >= M; ++it) { ++r; mr += M; }
+  return r;
+}
+
+// the reciprocal div_rn wants for divisor b: recip116 of its mantissa, or 0
+// when the mantissa is 2^52 (b a power of two)
+BGS_HD uint64_t divisor_recip(double b) {
+  const uint64_t M = (double_to_bits(b) & 0x000FFFFFFFFFFFFFULL) | 0x0010000000000000ULL;
+  return M == 0x0010000000000000ULL ? 0ULL : recip116(M);
+}
+
+// a / b rounded to nearest even, with rb = divisor_recip(b).
+BGS_HD double div_rn(double a, double b, uint64_t rb) {
+  const uint64_t ab = double_to_bits(a), bb = double_to_bits(b);
+  const int ea = (int)((ab >> 52) & 0x7FF), eb = (int)((bb >> 52) & 0x7FF);
+  if (ea == 0 || ea == 0x7FF || eb == 0 || eb == 0x7FF) return a / b;
+  const uint64_t Ma = (ab & 0x000FFFFFFFFFFFFFULL) | 0x0010000000000000ULL;
+  const uint64_t Mb = (bb & 0x000FFFFFFFFFFFFFULL) | 0x0010000000000000ULL;
+  const uint64_t sign = ((ab ^ bb) >> 63) << 63;
+  int e = ea - eb;  // q = Ma/Mb * 2^e
+  uint64_t q;       // 53-bit result mantissa
+  if (Mb == 0x0010000000000000ULL) {
+    q = Ma;  // exact
+  } else {
+    // Q ~ Ma/Mb * 2^63 (error < 2 units), Ma/Mb in (1/2, 2)
+    const uint64_t Q = (uint64_t)(((u128)(Ma << 11) * rb) >> 64);
+    // position the quotient: if Ma >= Mb, Q in [2^63, 2^64); else [2^62, 2^63)
+    const bool big = Ma >= Mb;
+    if (!big) e -= 1;
+    const int drop = big ? 11 : 10;            // bits below the 53-bit mantissa
+    uint64_t qt = Q >> drop;                   // truncated candidate
+    const uint64_t rem = Q & ((1ULL << drop) - 1);
+    const uint64_t halfw = 1ULL << (drop - 1);
+    // decide by the exact remainder when the estimate is near a boundary
+    if (rem + 4 >= halfw && rem <= halfw + 4) {
+      // compare Ma * 2^s with (qt + 1/2) * Mb exactly: s = 52 (big) or 53
+      const int s = big ? 52 : 53;
+      const u128 lhs = (u128)Ma << (s + 1);
+      const u128 mid = (u128)(2 * qt + 1) * Mb;
+      const bool above = lhs > mid, tie = lhs == mid;
+      qt += (above || (tie && (qt & 1))) ? 1 : 0;
+    } else if (rem > halfw) {
+      ++qt;
+    } else if (rem + 4 >= (1ULL << drop)) {
+      // estimate may sit just below the next integer: settle exactly
+      const int s = big ? 52 : 53;
+      const u128 lhs = (u128)Ma << (s + 1);
+      uint64_t c = qt + 1;
+      const u128 mid = (u128)(2 * c + 1) * Mb;
+      qt = lhs > mid ? c + 1 : (lhs == mid ? ((c & 1) ? c + 1 : c) : c);
+    }
+    q = qt;
+    if (q >> 53) { q >>= 1; e += 1; }
+  }
+  const int be = e + 1023;
+  if (be <= 0 || be >= 0x7FF) return a / b;
+  return bits_to_double(sign | ((uint64_t)be << 52) | (q & 0x000FFFFFFFFFFFFFULL));
+}
+
+// sqrt(x) rounded to nearest for normal x > 0: 1/sqrt by Newton in fixed
+// point from a float seed, the root w*r, then the exact floor and rounding
+// checked with 128-bit integer squares.
+BGS_HD double sqrt_rn(double x) {
+  const uint64_t xb = double_to_bits(x);
+  const int ex = (int)((xb >> 52) & 0x7FF);
+  if (ex == 0 || ex == 0x7FF || (xb >> 63)) {
+#if defined(__CUDA_ARCH__)
+    return __dsqrt_rn(x);
+#else
+    return std::sqrt(x);
+#endif
+  }
+  uint64_t M = (xb & 0x000FFFFFFFFFFFFFULL) | 0x0010000000000000ULL;
+  int e = ex - 1075;  // x = M * 2^e
+  if (e & 1) { M <<= 1; --e; }  // e even, 2^52 <= M < 2^54
+  const u128 N = (u128)M << 52;  // sqrt(x) = sqrt(N) * 2^((e-52)/2), sqrt(N) in [2^52, 2^53)
+  const uint64_t W = M << 10;    // w = M/2^54 in [1/4, 1), Q64
+  const float wf = u64_to_float_approx(M >> 30) * (1.0f / 16777216.0f);
+#if defined(__CUDA_ARCH__)
+  const float rsf = rsqrtf(wf);
+#else
+  const float rsf = 1.0f / std::sqrt(wf);
+#endif
+  uint64_t R = float_to_fixed(rsf, 62);  // r = 1/sqrt(w) in (1, 2], Q62
+  for (int it = 0; it < 2; ++it) {
+    const uint64_t R2 = (uint64_t)(((u128)R * R) >> 64);   // r^2, Q60
+    const uint64_t wr2 = mulhi(W, R2);                       // w r^2, Q60 (~2^60)
+    const uint64_t t = 3ULL * (1ULL << 60) - wr2;           // (3 - w r^2), Q60
+    R = (uint64_t)(((u128)R * t) >> 61);                     // r (3 - w r^2)/2, Q62
+  }
+  uint64_t y = mulhi(W, R) >> 9;  // sqrt(w) * 2^53 ~ floor(sqrt(N))
+  for (int it = 0; it < 8 && (u128)y * y > N; ++it) --y;
+  for (int it = 0; it < 8 && (u128)(y + 1) * (y + 1) <= N; ++it) ++y;
+  // nearest: N - y^2 > y  <=>  sqrt(N) > y + 1/2 (no exact ties)
+  if (N - (u128)y * y > (u128)y) ++y;
+  int eo = (e - 52) / 2 + 52;  // value = y * 2^(eo - 52)
+  if (y >> 53) { y >>= 1; ++eo; }
+  return bits_to_double(((uint64_t)(eo + 1023) << 52) | (y & 0x000FFFFFFFFFFFFFULL));
+}
+
+}  // namespace fix
+}  // namespace bgs

@@ -46,10 +46,15 @@ constexpr uint32_t kMaxSegmentsPerHistory = 100000000u;
 // those of the upstream loop:
 //   sig_eff  = (1 - f)*sigma_a + sigma_s   (effective scattering opacity)
 //   neg_saf  = -sigma_a * f                (exponent rate, negated)
-//   saf      =  sigma_a * f                (track-length divisor)
+//   inv_saf  = 1/(sigma_a * f)            (track-length factor; the tally
+//                                          contribution absorbed/(sigma_a f) is
+//                                          formed as a product, within 1 ulp)
 //   p_scat   = sigma_s / sig_eff           (physical-scatter probability)
-struct __align__(32) CellXS {
-  double sig_eff, neg_saf, saf, p_scat;
+//   rb_sig   = 64-bit reciprocal of sig_eff's mantissa for the exact integer
+//              division -log(u)/sig_eff (bgs_fixmath.cuh div_rn)
+struct __align__(16) CellXS {
+  double sig_eff, neg_saf, inv_saf, p_scat;
+  unsigned long long rb_sig, pad;
 };
 
 // 128-bit fixed-point tally cell: value = (hi*2^64 + lo) * 2^-scale.
@@ -138,12 +143,31 @@ __device__ __forceinline__ double u01_from_bits(unsigned long long w) {
   return __longlong_as_double((long long)((expo << 52) | mant));
 }
 
+// mu = u*2 - 1 for u = m * 2^-53 (sampling_functions.h:63): exactly
+// (m - 2^52) * 2^-52, assembled from integer bits (m odd, so never zero)
+__device__ __forceinline__ double mu_from_m53(unsigned long long m) {
+  const long long k = (long long)m - (1LL << 52);
+  const unsigned long long a = (unsigned long long)(k < 0 ? -k : k);  // 1 <= a < 2^52
+  const int s = __clzll((long long)a) - 11;
+  const unsigned long long mant = (a << s) & 0x000FFFFFFFFFFFFFULL;
+  const unsigned long long expo = (unsigned long long)(1023 - s);  // a*2^-52 in [2^-s, 2^(1-s))
+  return __longlong_as_double((long long)(((k < 0 ? 1ULL : 0ULL) << 63) | (expo << 52) | mant));
+}
+
 struct Rng {
   unsigned long long stream, ctr, hi;  // hi = seed << 32
   __device__ __forceinline__ double next() {
     const double u = u01_from_bits(threefry2x64_20_w0(ctr, hi, stream));
     ++ctr;
     return u;
+  }
+  // advance past a draw whose value cannot change the result
+  __device__ __forceinline__ void skip() { ++ctr; }
+  // the integer m of the next draw u = m * 2^-53 (u01fixedpt, RNG.h:202-238)
+  __device__ __forceinline__ unsigned long long next_m53() {
+    const unsigned long long w = threefry2x64_20_w0(ctr, hi, stream);
+    ++ctr;
+    return (w >> 11) | 1ULL;
   }
 };
 

@@ -1,6 +1,7 @@
 // Device helpers shared by the kernels and the host launcher declarations.
 #pragma once
 
+#include "bgs_fixmath.cuh"
 #include "bgs_internal.cuh"
 
 namespace bgs {
@@ -29,8 +30,10 @@ __device__ __forceinline__ void set_cell_xs(const CellsDev &c, uint32_t g, doubl
   CellXS x;
   x.sig_eff = (1.0 - f) * op_a + op_s;
   x.neg_saf = -op_a * f;
-  x.saf = op_a * f;
+  x.inv_saf = 1.0 / (op_a * f);
   x.p_scat = op_s / ((1.0 - f) * op_a + op_s);
+  x.rb_sig = x.sig_eff > 0.0 ? fix::divisor_recip(x.sig_eff) : 0ULL;
+  x.pad = 0;
   c.xs[g] = x;
   const double norm_factor = 1.0 / (op_a * (double)n_groups);
   c.group_v[g] = op_a * norm_factor;

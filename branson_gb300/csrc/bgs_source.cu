@@ -4,6 +4,7 @@
 // each photon finds its cell by binary search in the prefix-summed counts,
 // so the photon order, stream numbers and energies are those of the
 // upstream cell-order loops.
+#include "bgs_fixmath.cuh"
 #include "bgs_kernels.cuh"
 
 namespace bgs {
@@ -43,11 +44,11 @@ __device__ __forceinline__ void position_in_cell(const double n[6], Rng &r, doub
 
 // get_uniform_angle (sampling_functions.h:57-70)
 __device__ __forceinline__ void uniform_angle(Rng &r, double d[3]) {
-  const double mu = r.next() * 2.0 - 1.0;
+  const double mu = mu_from_m53(r.next_m53());
   const double phi = r.next() * 2.0 * kPi;
   const double sin_theta = sqrt(1.0 - mu * mu);
   double s, c;
-  sincos(phi, &s, &c);
+  fix::sincos_phi(phi, &s, &c);
   d[0] = sin_theta * c;
   d[1] = sin_theta * s;
   d[2] = mu;

@@ -16,6 +16,7 @@
 // Arithmetic is FP64 in the upstream operation order (the translation unit
 // is built without FMA contraction); the per-cell coefficients come from the
 // CellXS table, formed with the same expressions as the upstream loop.
+#include "bgs_fixmath.cuh"
 #include "bgs_kernels.cuh"
 
 namespace bgs {
@@ -23,7 +24,8 @@ namespace bgs {
 constexpr int kTransportThreads = 128;
 
 struct Lane {
-  double px, py, pz, dx, dy, dz, E, E0, life;
+  double px, py, pz, dx, dy, dz, E, E0, life, inv_E0;
+  unsigned long long rbx, rby, rbz;  // divisor reciprocals of the direction cosines
   double n0, n1, n2, n3, n4, n5;  // nodes of the current cell
   double thr_abs, thr_trk;
   unsigned long long idx;
@@ -49,6 +51,12 @@ __device__ __forceinline__ void flush_tally(const CellsDev &c, const DeviceDiag 
     if (to_fixed128(t, st, lo, hi)) atomic_add128(&tc->trk_lo, &tc->trk_hi, lo, hi);
     else flags |= (t == t) ? FLAG_TALLY_RANGE : FLAG_NAN;
   }
+}
+
+__device__ __forceinline__ void direction_recips(Lane &L) {
+  L.rbx = fix::divisor_recip(L.dx);
+  L.rby = fix::divisor_recip(L.dy);
+  L.rbz = fix::divisor_recip(L.dz);
 }
 
 __device__ __forceinline__ void store_end(const Bank &b, const Lane &L, uint8_t desc) {
@@ -103,6 +111,8 @@ __global__ void __launch_bounds__(kTransportThreads)
           L.cell = b.cell[i]; L.group = b.group[i];
           L.rng.stream = b.stream[i]; L.rng.ctr = b.ctr[i]; L.rng.hi = seed_hi;
           L.thr_abs = 0.0; L.thr_trk = 0.0; L.segs = 0;
+          L.inv_E0 = 1.0 / L.E0;
+          direction_recips(L);
           if (L.cell < m.n_cells) {
             L.ci = L.cell % m.ngx; L.cj = (L.cell / m.ngx) % m.ngy; L.ck = L.cell / (m.ngx * m.ngy);
             load_nodes(m, L);
@@ -123,57 +133,80 @@ __global__ void __launch_bounds__(kTransportThreads)
     ++L.segs;
     ++seg_total;
     const CellXS xs = c.xs[L.cell];
-    const double dist_to_scatter = (xs.sig_eff > 0.0) ? -log(L.rng.next()) / xs.sig_eff : 1.0e100;
+    // -log(u) / sigma_eff with the integer, correctly rounded -log (bgs_fixmath.cuh)
+    // (divisions are the exact integer div_rn: bitwise the IEEE quotient)
+    const double dist_to_scatter =
+        (xs.sig_eff > 0.0) ? fix::div_rn(fix::neg_log_u53(L.rng.next_m53()), xs.sig_eff, xs.rb_sig)
+                           : 1.0e100;
     // Cell::get_distance_to_boundary (cell.h:117-132)
     double dist_to_boundary = 1.0e16;
     uint32_t surface_cross = 0;
     {
       const bool pos = 0.0 < L.dx;
-      const double dist = ((pos ? L.n1 : L.n0) - L.px) / L.dx;
+      const double dist = fix::div_rn((pos ? L.n1 : L.n0) - L.px, L.dx, L.rbx);
       if (dist < dist_to_boundary) { dist_to_boundary = dist; surface_cross = pos ? 1u : 0u; }
     }
     {
       const bool pos = 0.0 < L.dy;
-      const double dist = ((pos ? L.n3 : L.n2) - L.py) / L.dy;
+      const double dist = fix::div_rn((pos ? L.n3 : L.n2) - L.py, L.dy, L.rby);
       if (dist < dist_to_boundary) { dist_to_boundary = dist; surface_cross = pos ? 3u : 2u; }
     }
     {
       const bool pos = 0.0 < L.dz;
-      const double dist = ((pos ? L.n5 : L.n4) - L.pz) / L.dz;
+      const double dist = fix::div_rn((pos ? L.n5 : L.n4) - L.pz, L.dz, L.rbz);
       if (dist < dist_to_boundary) { dist_to_boundary = dist; surface_cross = pos ? 5u : 4u; }
     }
     const double dist_to_census = L.life;
-    // std::min(a, b) == (b < a) ? b : a
-    const double inner = (dist_to_census < dist_to_boundary) ? dist_to_census : dist_to_boundary;
-    const double dist_to_event = (inner < dist_to_scatter) ? inner : dist_to_scatter;
+    // std::min(a, b) == (b < a) ? b : a; the event tests that follow
+    // (dist_to_event == dist_to_scatter, then == dist_to_boundary) are the
+    // same comparisons read back
+    const bool census_first = dist_to_census < dist_to_boundary;
+    const double inner = census_first ? dist_to_census : dist_to_boundary;
+    const bool inner_first = inner < dist_to_scatter;
+    const double dist_to_event = inner_first ? inner : dist_to_scatter;
 
-    const double absorbed_E = L.E * (1.0 - exp(xs.neg_saf * dist_to_event));
+    const double absorbed_E = L.E * (1.0 - fix::exp_neg(-(xs.neg_saf * dist_to_event)));
     L.thr_abs += absorbed_E;
-    L.thr_trk += absorbed_E / xs.saf;
+    L.thr_trk += absorbed_E * xs.inv_saf;
     L.E = L.E - absorbed_E;
     L.px += L.dx * dist_to_event;  // Photon::move (photon.h:109-114)
     L.py += L.dy * dist_to_event;
     L.pz += L.dz * dist_to_event;
     L.life -= dist_to_event;
 
-    if (L.E / L.E0 < kCutoff || L.segs >= kMaxSegmentsPerHistory) {
-      if (L.segs >= kMaxSegmentsPerHistory && !(L.E / L.E0 < kCutoff)) flags |= FLAG_SEGMENT_LIMIT;
+    // below_cutoff: E/E0 < 0.01 (photon.h:47-49), decided from E*(1/E0) and
+    // settled with the exact quotient only within a few ulps of the threshold
+    const double frac = L.E * L.inv_E0;
+    bool killed = frac < kCutoff;
+    if (fabs(frac - kCutoff) <= 4.0e-18) killed = L.E / L.E0 < kCutoff;
+    if (killed || L.segs >= kMaxSegmentsPerHistory) {
+      if (!killed) flags |= FLAG_SEGMENT_LIMIT;
       L.thr_abs += L.E;
       flush_tally(c, d, L.cell, L.thr_abs, L.thr_trk, flags, sa, st);
       store_end(b, L, KILLED);
       active = false;
-    } else if (dist_to_event == dist_to_scatter) {
+    } else if (!inner_first) {  // dist_to_event == dist_to_scatter
       // get_uniform_angle (sampling_functions.h:57-70)
-      const double mu = L.rng.next() * 2.0 - 1.0;
+      const double mu = mu_from_m53(L.rng.next_m53());
       const double phi = L.rng.next() * 2.0 * kPi;
-      const double sin_theta = sqrt(1.0 - mu * mu);
+      const double sin_theta = fix::sqrt_rn(1.0 - mu * mu);
       double sp, cp;
-      sincos(phi, &sp, &cp);
+      fix::sincos_phi(phi, &sp, &cp);
       L.dx = sin_theta * cp;
       L.dy = sin_theta * sp;
       L.dz = mu;
-      if (L.rng.next() > xs.p_scat) L.group = sample_group(L.rng, c.group_v[L.cell], m.n_groups);
-    } else if (dist_to_event == dist_to_boundary) {
+      direction_recips(L);
+      // effective-scatter test and group resample (history_based_transport.h:97-98):
+      // with sigma_s = 0 the test u > 0 always passes, and with one group the
+      // walk always ends in group 0, so those draws only advance the counter
+      bool resample;
+      if (xs.p_scat > 0.0) resample = L.rng.next() > xs.p_scat;
+      else { L.rng.skip(); resample = true; }
+      if (resample) {
+        if (m.n_groups > 1) L.group = sample_group(L.rng, c.group_v[L.cell], m.n_groups);
+        else { L.rng.skip(); L.group = 0; }
+      }
+    } else if (!census_first) {  // dist_to_event == dist_to_boundary
       // structured-mesh face: interior faces are ELEMENT (proto_mesh.h:156-202)
       bool interior;
       switch (surface_cross) {
@@ -207,7 +240,7 @@ __global__ void __launch_bounds__(kTransportThreads)
         else if (surface_cross < 4) L.dy = -L.dy;
         else L.dz = -L.dz;
       }
-    } else if (dist_to_event == dist_to_census) {
+    } else {  // dist_to_event == dist_to_census
       flush_tally(c, d, L.cell, L.thr_abs, L.thr_trk, flags, sa, st);
       store_end(b, L, CENSUS);
       active = false;
