@@ -14,7 +14,7 @@ import numpy as np
 
 from . import build as _build
 
-LIB_PATH = _build.LIB
+LIB_PATH = os.environ.get("BRANSON_GB300_LIB", _build.LIB)
 
 OK, ERR_INVALID, ERR_CUDA, ERR_CAPACITY, ERR_STATE, ERR_DEVICE, ERR_NO_DEVICE = range(7)
 REFLECT, VACUUM, ELEMENT, SOURCE, PROCESSOR = range(5)

@@ -32,8 +32,13 @@
 
 #if defined(__CUDACC__)
 #define BGS_HD __host__ __device__ __forceinline__
+// one shared copy in device code: routines called from several places of
+// the transport loop are kept out of line so the loop fits the instruction
+// cache
+#define BGS_HD_SHARED static __host__ __device__ __noinline__
 #else
 #define BGS_HD inline
+#define BGS_HD_SHARED inline
 #endif
 
 namespace bgs {
@@ -112,7 +117,7 @@ BGS_HD uint64_t double_to_bits(double d) {
 // Round the positive value W * 2^-scale (W != 0) to the nearest double.
 // Values below the normal range flush to zero (callers never produce them
 // on the paths that use this).
-BGS_HD double round_u128(u128 W, int scale) {
+BGS_HD_SHARED double round_u128(u128 W, int scale) {
   const uint64_t hi = (uint64_t)(W >> 64), lo = (uint64_t)W;
   const int p = hi ? 127 - clz64(hi) : 63 - clz64(lo);  // top set bit
   uint64_t mant;
@@ -197,8 +202,10 @@ BGS_HD double exp_neg(double tau) {
   uint64_t N = mulhi(A, fixtab::kInvLn2_1024_q12);
   const u128 L = ((u128)fixtab::kLn2_1024_96_hi << 64) | fixtab::kLn2_1024_96_lo;
   u128 NL = L * N;
+#pragma unroll 1
   for (int it = 0; it < 4 && NL > T; ++it) { --N; NL -= L; }
   u128 S = T - NL;
+#pragma unroll 1
   for (int it = 0; it < 4 && S >= L; ++it) { ++N; S -= L; }
   // s * 2^73 (s < ln2/1024 < 2^-10.5)
   const uint64_t s73 = (uint64_t)(S >> 23);
@@ -342,7 +349,7 @@ BGS_HD float u64_to_float_approx(uint64_t x) {  // x < 2^24, exact
 // floor(2^116 / M) for a 53-bit mantissa M in (2^52, 2^53): a 64-bit
 // reciprocal, from a float seed refined by two Newton steps in fixed point
 // and corrected to the exact floor.
-BGS_HD uint64_t recip116(uint64_t M) {
+BGS_HD_SHARED uint64_t recip116(uint64_t M) {
   const float mf = u64_to_float_approx(M >> 29);  // M / 2^29, 24 bits
 #if defined(__CUDA_ARCH__)
   const float rf = __frcp_rn(mf);
@@ -351,6 +358,7 @@ BGS_HD uint64_t recip116(uint64_t M) {
 #endif
   uint64_t r = float_to_fixed(rf, 87);  // ~2^116/M
   // Newton: r <- r (2 - M r / 2^116) in fixed point, twice
+#pragma unroll 1
   for (int it = 0; it < 2; ++it) {
     const u128 mr = (u128)M * r;
     const u128 err = (((u128)1) << 117) - mr;  // (2 - M r/2^116) * 2^116
@@ -359,7 +367,9 @@ BGS_HD uint64_t recip116(uint64_t M) {
   // exact correction to floor(2^116/M)
   const u128 P = ((u128)1) << 116;
   u128 mr = (u128)M * r;
+#pragma unroll 1
   for (int it = 0; it < 8 && mr > P; ++it) { --r; mr -= M; }
+#pragma unroll 1
   for (int it = 0; it < 8 && P - mr >= M; ++it) { ++r; mr += M; }
   return r;
 }
@@ -369,6 +379,21 @@ BGS_HD uint64_t recip116(uint64_t M) {
 BGS_HD uint64_t divisor_recip(double b) {
   const uint64_t M = (double_to_bits(b) & 0x000FFFFFFFFFFFFFULL) | 0x0010000000000000ULL;
   return M == 0x0010000000000000ULL ? 0ULL : recip116(M);
+}
+
+// settle the rounding of Ma/Mb exactly: the candidate qt (53 bits) is
+// compared with the true quotient through 128-bit products; c_hi asks whether
+// the estimate may sit just below qt + 1
+BGS_HD_SHARED uint64_t div_settle(uint64_t Ma, uint64_t Mb, uint64_t qt, int s, bool next) {
+  const u128 lhs = (u128)Ma << (s + 1);
+  if (next) {
+    const uint64_t c = qt + 1;
+    const u128 mid = (u128)(2 * c + 1) * Mb;
+    return lhs > mid ? c + 1 : (lhs == mid ? ((c & 1) ? c + 1 : c) : c);
+  }
+  const u128 mid = (u128)(2 * qt + 1) * Mb;
+  const bool above = lhs > mid, tie = lhs == mid;
+  return qt + ((above || (tie && (qt & 1))) ? 1 : 0);
 }
 
 // a / b rounded to nearest even, with rb = divisor_recip(b).
@@ -393,23 +418,14 @@ BGS_HD double div_rn(double a, double b, uint64_t rb) {
     uint64_t qt = Q >> drop;                   // truncated candidate
     const uint64_t rem = Q & ((1ULL << drop) - 1);
     const uint64_t halfw = 1ULL << (drop - 1);
-    // decide by the exact remainder when the estimate is near a boundary
+    // decide by the exact remainder when the estimate is near a boundary:
+    // compare Ma * 2^s with (qt + 1/2) * Mb, s = 52 (big) or 53
     if (rem + 4 >= halfw && rem <= halfw + 4) {
-      // compare Ma * 2^s with (qt + 1/2) * Mb exactly: s = 52 (big) or 53
-      const int s = big ? 52 : 53;
-      const u128 lhs = (u128)Ma << (s + 1);
-      const u128 mid = (u128)(2 * qt + 1) * Mb;
-      const bool above = lhs > mid, tie = lhs == mid;
-      qt += (above || (tie && (qt & 1))) ? 1 : 0;
+      qt = div_settle(Ma, Mb, qt, big ? 52 : 53, false);
     } else if (rem > halfw) {
       ++qt;
     } else if (rem + 4 >= (1ULL << drop)) {
-      // estimate may sit just below the next integer: settle exactly
-      const int s = big ? 52 : 53;
-      const u128 lhs = (u128)Ma << (s + 1);
-      uint64_t c = qt + 1;
-      const u128 mid = (u128)(2 * c + 1) * Mb;
-      qt = lhs > mid ? c + 1 : (lhs == mid ? ((c & 1) ? c + 1 : c) : c);
+      qt = div_settle(Ma, Mb, qt, big ? 52 : 53, true);
     }
     q = qt;
     if (q >> 53) { q >>= 1; e += 1; }
@@ -444,6 +460,7 @@ BGS_HD double sqrt_rn(double x) {
   const float rsf = 1.0f / std::sqrt(wf);
 #endif
   uint64_t R = float_to_fixed(rsf, 62);  // r = 1/sqrt(w) in (1, 2], Q62
+#pragma unroll 1
   for (int it = 0; it < 2; ++it) {
     const uint64_t R2 = (uint64_t)(((u128)R * R) >> 64);   // r^2, Q60
     const uint64_t wr2 = mulhi(W, R2);                       // w r^2, Q60 (~2^60)
@@ -451,7 +468,9 @@ BGS_HD double sqrt_rn(double x) {
     R = (uint64_t)(((u128)R * t) >> 61);                     // r (3 - w r^2)/2, Q62
   }
   uint64_t y = mulhi(W, R) >> 9;  // sqrt(w) * 2^53 ~ floor(sqrt(N))
+#pragma unroll 1
   for (int it = 0; it < 8 && (u128)y * y > N; ++it) --y;
+#pragma unroll 1
   for (int it = 0; it < 8 && (u128)(y + 1) * (y + 1) <= N; ++it) ++y;
   // nearest: N - y^2 > y  <=>  sqrt(N) > y + 1/2 (no exact ties)
   if (N - (u128)y * y > (u128)y) ++y;

@@ -22,6 +22,50 @@
 namespace bgs {
 
 constexpr int kTransportThreads = 128;
+// Build-time choices for the per-segment arithmetic (see the header comment
+// of bgs_fixmath.cuh): integer or FP64 for the divisions, the square root
+// and sin/cos, and the minimum number of resident blocks per SM.
+#ifndef BGS_INT_DIV
+#define BGS_INT_DIV 0
+#endif
+#ifndef BGS_INT_SQRT
+#define BGS_INT_SQRT 1
+#endif
+#ifndef BGS_INT_SINCOS
+#define BGS_INT_SINCOS 1
+#endif
+#ifndef BGS_MIN_BLOCKS
+#define BGS_MIN_BLOCKS 5
+#endif
+#ifndef BGS_INT_DIV_DS
+#define BGS_INT_DIV_DS 0  // -log(u)/sigma_eff by the exact integer division (per-cell reciprocal)
+#endif
+#ifndef BGS_SPEC_DRAWS
+#define BGS_SPEC_DRAWS 0  // draw the scattering angles with the collision distance (3 at once)
+#endif
+
+__device__ __forceinline__ double seg_div(double a, double b, unsigned long long rb) {
+#if BGS_INT_DIV
+  return fix::div_rn(a, b, rb);
+#else
+  (void)rb;
+  return a / b;
+#endif
+}
+__device__ __forceinline__ double seg_sqrt(double x) {
+#if BGS_INT_SQRT
+  return fix::sqrt_rn(x);
+#else
+  return sqrt(x);
+#endif
+}
+__device__ __forceinline__ void seg_sincos(double phi, double *s, double *c) {
+#if BGS_INT_SINCOS
+  fix::sincos_phi(phi, s, c);
+#else
+  sincos(phi, s, c);
+#endif
+}
 
 struct Lane {
   double px, py, pz, dx, dy, dz, E, E0, life, inv_E0;
@@ -54,9 +98,14 @@ __device__ __forceinline__ void flush_tally(const CellsDev &c, const DeviceDiag 
 }
 
 __device__ __forceinline__ void direction_recips(Lane &L) {
+
+#if BGS_INT_DIV
   L.rbx = fix::divisor_recip(L.dx);
   L.rby = fix::divisor_recip(L.dy);
   L.rbz = fix::divisor_recip(L.dz);
+#else
+  (void)L;
+#endif
 }
 
 __device__ __forceinline__ void store_end(const Bank &b, const Lane &L, uint8_t desc) {
@@ -82,7 +131,7 @@ __device__ __forceinline__ uint32_t sample_group(Rng &r, double v, uint32_t n_gr
   return g < 0 ? 0u : (uint32_t)g;
 }
 
-__global__ void __launch_bounds__(kTransportThreads)
+__global__ void __launch_bounds__(kTransportThreads, BGS_MIN_BLOCKS)
     k_transport_history(MeshDev m, CellsDev c, Bank b, DeviceDiag *d, unsigned long long seed_hi) {
   const unsigned long long n = d->n_bank;
   const int sa = d->scale_abs, st = d->scale_track;
@@ -135,26 +184,42 @@ __global__ void __launch_bounds__(kTransportThreads)
     const CellXS xs = c.xs[L.cell];
     // -log(u) / sigma_eff with the integer, correctly rounded -log (bgs_fixmath.cuh)
     // (divisions are the exact integer div_rn: bitwise the IEEE quotient)
+#if BGS_SPEC_DRAWS
+    // the collision draw and, speculatively, the two angle draws that a
+    // scatter would take next: three independent Threefry evaluations
+    unsigned long long w_mu = 0, w_phi = 0;
+    unsigned long long m_ds = 0;
+    if (xs.sig_eff > 0.0) {
+      const unsigned long long w0 = L.rng.peek(0);
+      w_mu = L.rng.peek(1);
+      w_phi = L.rng.peek(2);
+      L.rng.skip();
+      m_ds = (w0 >> 11) | 1ULL;
+    }
+    const double dist_to_scatter =
+        (xs.sig_eff > 0.0) ? fix::div_rn(fix::neg_log_u53(m_ds), xs.sig_eff, xs.rb_sig) : 1.0e100;
+#elif BGS_INT_DIV_DS
     const double dist_to_scatter =
         (xs.sig_eff > 0.0) ? fix::div_rn(fix::neg_log_u53(L.rng.next_m53()), xs.sig_eff, xs.rb_sig)
                            : 1.0e100;
+#else
+    const double dist_to_scatter =
+        (xs.sig_eff > 0.0) ? fix::neg_log_u53(L.rng.next_m53()) / xs.sig_eff : 1.0e100;
+#endif
     // Cell::get_distance_to_boundary (cell.h:117-132)
     double dist_to_boundary = 1.0e16;
     uint32_t surface_cross = 0;
+    const bool posx = 0.0 < L.dx, posy = 0.0 < L.dy, posz = 0.0 < L.dz;
+    const double numx = (posx ? L.n1 : L.n0) - L.px;
+    const double numy = (posy ? L.n3 : L.n2) - L.py;
+    const double numz = (posz ? L.n5 : L.n4) - L.pz;
     {
-      const bool pos = 0.0 < L.dx;
-      const double dist = fix::div_rn((pos ? L.n1 : L.n0) - L.px, L.dx, L.rbx);
-      if (dist < dist_to_boundary) { dist_to_boundary = dist; surface_cross = pos ? 1u : 0u; }
-    }
-    {
-      const bool pos = 0.0 < L.dy;
-      const double dist = fix::div_rn((pos ? L.n3 : L.n2) - L.py, L.dy, L.rby);
-      if (dist < dist_to_boundary) { dist_to_boundary = dist; surface_cross = pos ? 3u : 2u; }
-    }
-    {
-      const bool pos = 0.0 < L.dz;
-      const double dist = fix::div_rn((pos ? L.n5 : L.n4) - L.pz, L.dz, L.rbz);
-      if (dist < dist_to_boundary) { dist_to_boundary = dist; surface_cross = pos ? 5u : 4u; }
+      double dist = seg_div(numx, L.dx, L.rbx);
+      if (dist < dist_to_boundary) { dist_to_boundary = dist; surface_cross = posx ? 1u : 0u; }
+      dist = seg_div(numy, L.dy, L.rby);
+      if (dist < dist_to_boundary) { dist_to_boundary = dist; surface_cross = posy ? 3u : 2u; }
+      dist = seg_div(numz, L.dz, L.rbz);
+      if (dist < dist_to_boundary) { dist_to_boundary = dist; surface_cross = posz ? 5u : 4u; }
     }
     const double dist_to_census = L.life;
     // std::min(a, b) == (b < a) ? b : a; the event tests that follow
@@ -187,11 +252,18 @@ __global__ void __launch_bounds__(kTransportThreads)
       active = false;
     } else if (!inner_first) {  // dist_to_event == dist_to_scatter
       // get_uniform_angle (sampling_functions.h:57-70)
+#if BGS_SPEC_DRAWS
+      const double mu = mu_from_m53((w_mu >> 11) | 1ULL);
+      const double phi = u01_from_bits(w_phi) * 2.0 * kPi;
+      L.rng.skip();
+      L.rng.skip();
+#else
       const double mu = mu_from_m53(L.rng.next_m53());
       const double phi = L.rng.next() * 2.0 * kPi;
-      const double sin_theta = fix::sqrt_rn(1.0 - mu * mu);
+#endif
+      const double sin_theta = seg_sqrt(1.0 - mu * mu);
       double sp, cp;
-      fix::sincos_phi(phi, &sp, &cp);
+      seg_sincos(phi, &sp, &cp);
       L.dx = sin_theta * cp;
       L.dy = sin_theta * sp;
       L.dz = mu;
