@@ -89,6 +89,10 @@ SIGNATURES = (
     ("bgs_replicated_transport", C.c_int,
      [C.c_void_p, C.c_uint64, C.POINTER(PhotonsHost), C.c_double, C.c_uint32, C.c_void_p, C.c_void_p,
       C.POINTER(PhotonsHost), C.c_uint64, C.POINTER(C.c_uint64), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    ("bgs_transport_device_noalloc", C.c_int,
+     [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
+      C.POINTER(C.c_int32), C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint64,
+      C.POINTER(PhotonsHost), C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("bgs_last_transport_ms", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_uint32)]),
     ("bgs_kernel_launch_count", C.c_uint64, [C.c_void_p]),
 )

@@ -186,6 +186,35 @@ BGS_API int bgs_replicated_transport(bgs_context *ctx, uint64_t n, const bgs_pho
                              uint64_t census_capacity, uint64_t *n_census, double *census_E,
                              double *exit_E);
 
+/* ------------------------------------------- transport without allocation */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory -- host codes that own every device byte through their own pool
+ * allocator, or code that must not trigger a cudaMalloc/cudaFree between
+ * its launches: the history transport of bgs_replicated_transport on device
+ * buffers the caller owns, with all scratch (fixed-point tallies, the
+ * per-cell table, counters) in one static device array of the library, so
+ * the call allocates nothing.
+ *   x/y/z_planes   device, ngx+1 / ngy+1 / ngz+1 node planes
+ *   bc             host, 6 domain boundary codes (REFLECT, VACUUM, SOURCE)
+ *   op_a, op_s, f  device, one value per cell (cell g = i + ngx*(j + ngy*k))
+ *   photons        device structure of arrays, n photons, updated in place
+ *                  with their end states; CENSUS photons get life_dx =
+ *                  c*next_dt (no compaction: the census stays in place)
+ *   abs_E, track_E device outputs, one value per cell (overwritten)
+ *   stream         cudaStream_t (NULL: the legacy default stream)
+ * Limit: at most 131072 cells (BGS_ERR_CAPACITY beyond); the array (about
+ * 11 MB) is held by every GPU that loads the library until exit.  The first
+ * call on a device looks up the array's address, so it must come before
+ * any stream capture.  All calls share the array: calls that overlap on the
+ * GPU race.  Returns after the work completes (BGS_ERR_DEVICE if a device
+ * check fired). */
+BGS_API int bgs_transport_device_noalloc(uint32_t ngx, uint32_t ngy, uint32_t ngz, uint32_t n_groups,
+                                         const double *x_planes, const double *y_planes,
+                                         const double *z_planes, const int32_t bc[6], const double *op_a,
+                                         const double *op_s, const double *f, uint32_t seed, uint64_t n,
+                                         const bgs_photons_host *photons, double next_dt, double *abs_E,
+                                         double *track_E, void *stream);
+
 /* ------------------------------------------------------- instrumentation */
 /* Device time (ms) of the last transport kernel span, measured with CUDA
  * events on the context's stream, and its launch count. */
