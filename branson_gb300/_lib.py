@@ -20,6 +20,7 @@ OK, ERR_INVALID, ERR_CUDA, ERR_CAPACITY, ERR_STATE, ERR_DEVICE, ERR_NO_DEVICE = 
 REFLECT, VACUUM, ELEMENT, SOURCE, PROCESSOR = range(5)
 EXIT, PASS, CENSUS, SCATTER, KILLED, BOUND = range(6)
 HISTORY, EVENT = 0, 1
+OPTIONS = {"event_round_cap": 0, "event_check_every": 1, "event_tail_fraction": 2, "transport_blocks": 3}
 FIELDS = {"T_e": 0, "T_r": 1, "op_a": 2, "op_s": 3, "f": 4, "emission_E": 5, "census_E": 6,
           "source_E": 7, "abs_E": 8, "track_E": 9}
 
@@ -93,6 +94,7 @@ SIGNATURES = (
      [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
       C.POINTER(C.c_int32), C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint64,
       C.POINTER(PhotonsHost), C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("bgs_set_option", C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     ("bgs_last_transport_ms", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_uint32)]),
     ("bgs_kernel_launch_count", C.c_uint64, [C.c_void_p]),
 )

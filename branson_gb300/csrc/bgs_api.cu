@@ -37,6 +37,15 @@ struct bgs_context {
   std::vector<void *> bank_allocs;
   unsigned long long *d_off_bank = nullptr, *d_tile_bank = nullptr, *d_maxbits = nullptr;
 
+  // event mode (allocated on first use): carried tallies, surfaces, lists, counters
+  std::vector<void *> event_allocs;
+  EventState ev_a{}, ev_b{};     // ev_b has active/next swapped
+  unsigned int *h_counter = nullptr;  // pinned
+  uint32_t event_round_cap = 64;      // rounds before the tail goes to the history kernel
+  uint32_t event_check_every = 4;     // rounds between host reads of the active count
+  double event_tail_fraction = 0.02;  // active share below which the tail goes to history mode
+  unsigned long long last_event_rounds = 0;
+
   DeviceDiag *d_diag = nullptr;
   DeviceDiag *h_diag = nullptr;  // pinned
   TransportLaunch tshape{};
@@ -282,6 +291,8 @@ int bgs_destroy(bgs_context *ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   free_list(ctx->mesh_allocs);
   free_list(ctx->bank_allocs);
+  free_list(ctx->event_allocs);
+  if (ctx->h_counter) cudaFreeHost(ctx->h_counter);
   if (ctx->d_diag) cudaFree(ctx->d_diag);
   if (ctx->h_diag) cudaFreeHost(ctx->h_diag);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -440,6 +451,71 @@ int bgs_source(bgs_context *ctx, uint32_t step, double dt) {
   return BGS_OK;
 }
 
+static int ensure_event_state(bgs_context *ctx) {
+  if (ctx->ev_a.active) return BGS_OK;
+  const unsigned long long cap = ctx->capacity;
+  EventState e{};
+  int rc;
+  auto &L = ctx->event_allocs;
+  if ((rc = dev_alloc(ctx, L, &e.thr_abs, cap)) || (rc = dev_alloc(ctx, L, &e.thr_trk, cap)) ||
+      (rc = dev_alloc(ctx, L, &e.surface, cap)) || (rc = dev_alloc(ctx, L, &e.active, cap)) ||
+      (rc = dev_alloc(ctx, L, &e.next, cap)) || (rc = dev_alloc(ctx, L, &e.q_scatter, cap)) ||
+      (rc = dev_alloc(ctx, L, &e.q_boundary, cap)))
+    return rc;
+  unsigned int *cnt;
+  if ((rc = dev_alloc(ctx, L, &cnt, 4))) return rc;
+  e.n_active = cnt; e.n_next = cnt + 1; e.n_scatter = cnt + 2; e.n_boundary = cnt + 3;
+  if (!ctx->h_counter && cudaMallocHost(&ctx->h_counter, sizeof(unsigned int)) != cudaSuccess)
+    return fail(ctx, BGS_ERR_CUDA, "cudaMallocHost failed");
+  ctx->ev_a = e;
+  ctx->ev_b = e;
+  ctx->ev_b.active = e.next;
+  ctx->ev_b.next = e.active;
+  return BGS_OK;
+}
+
+// Event mode: stage rounds while the active set is large, then the history
+// kernel finishes the tail from the carried state.
+static int transport_event(bgs_context *ctx, const Bank &from) {
+  int rc;
+  if ((rc = ensure_event_state(ctx))) return rc;
+  launch_event_init(ctx->ev_a, ctx->d_diag, ctx->stream);
+  BGS_LAUNCHED(ctx, 1);
+  BGS_CUDA(ctx, cudaMemcpyAsync(ctx->h_counter, ctx->ev_a.n_active, sizeof(unsigned int),
+                                cudaMemcpyDeviceToHost, ctx->stream));
+  BGS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  const double n0 = (double)*ctx->h_counter;
+  const double tail = n0 * ctx->event_tail_fraction;
+  uint32_t round = 0;
+  unsigned int active = *ctx->h_counter;
+  while (active > 0 && round < ctx->event_round_cap && (double)active >= tail) {
+    const EventState &es = (round & 1) ? ctx->ev_b : ctx->ev_a;
+    launch_event_round(ctx->mesh, ctx->cells, from, ctx->d_diag, ctx->seed, es, round == 0, ctx->n_sm,
+                       ctx->stream);
+    BGS_LAUNCHED(ctx, 4);
+    ++round;
+    if (round % ctx->event_check_every == 0) {
+      BGS_CUDA(ctx, cudaMemcpyAsync(ctx->h_counter, ctx->ev_a.n_active, sizeof(unsigned int),
+                                    cudaMemcpyDeviceToHost, ctx->stream));
+      BGS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      active = *ctx->h_counter;
+    }
+  }
+  ctx->last_event_rounds = round;
+  // the survivors are in the list the last round wrote (its `next`)
+  const EventState &tail_es = (round & 1) ? ctx->ev_b : ctx->ev_a;
+  if (round == 0) {
+    launch_transport_history(ctx->mesh, ctx->cells, from, ctx->d_diag, ctx->seed, ctx->tshape, ctx->stream);
+  } else {
+    k_reset_queue<<<1, 1, 0, ctx->stream>>>(ctx->d_diag);
+    BGS_LAUNCHED(ctx, 1);
+    launch_transport_resume(ctx->mesh, ctx->cells, from, ctx->d_diag, ctx->seed, tail_es, ctx->tshape,
+                            ctx->stream);
+  }
+  BGS_LAUNCHED(ctx, 1);
+  return BGS_OK;
+}
+
 static int transport_impl(bgs_context *ctx, double next_dt, uint32_t algorithm, bool read_back) {
   if (algorithm != BGS_HISTORY && algorithm != BGS_EVENT)
     return fail(ctx, BGS_ERR_INVALID, "unknown transport algorithm %u", algorithm);
@@ -457,8 +533,13 @@ static int transport_impl(bgs_context *ctx, double next_dt, uint32_t algorithm, 
   k_reset_queue<<<1, 1, 0, ctx->stream>>>(ctx->d_diag);
   BGS_LAUNCHED(ctx, 1);
   BGS_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
-  launch_transport_history(ctx->mesh, ctx->cells, from, ctx->d_diag, ctx->seed, ctx->tshape, ctx->stream);
-  BGS_LAUNCHED(ctx, 1);
+  if (algorithm == BGS_EVENT) {
+    int rc;
+    if ((rc = transport_event(ctx, from))) return rc;
+  } else {
+    launch_transport_history(ctx->mesh, ctx->cells, from, ctx->d_diag, ctx->seed, ctx->tshape, ctx->stream);
+    BGS_LAUNCHED(ctx, 1);
+  }
   BGS_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
   launch_scan_flags(from.desc, CENSUS, (uint32_t)ctx->capacity, &ctx->d_diag->n_bank, ctx->d_off_bank,
                     ctx->d_tile_bank, ctx->stream);
@@ -602,6 +683,32 @@ int bgs_replicated_transport(bgs_context *ctx, uint64_t n, const bgs_photons_hos
     BGS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   }
   return BGS_OK;
+}
+
+int bgs_set_option(bgs_context *ctx, int option, double value) {
+  if (!ctx) return BGS_ERR_INVALID;
+  switch (option) {
+    case BGS_OPT_EVENT_ROUND_CAP:
+      if (!(value >= 0 && value <= 1e6)) break;
+      ctx->event_round_cap = (uint32_t)value;
+      return BGS_OK;
+    case BGS_OPT_EVENT_CHECK_EVERY:
+      if (!(value >= 1 && value <= 1e6)) break;
+      ctx->event_check_every = (uint32_t)value;
+      return BGS_OK;
+    case BGS_OPT_EVENT_TAIL_FRACTION:
+      if (!(value >= 0 && value <= 1)) break;
+      ctx->event_tail_fraction = value;
+      return BGS_OK;
+    case BGS_OPT_TRANSPORT_BLOCKS:
+      if (!(value >= 0 && value <= 1e6)) break;
+      ctx->tshape = transport_launch_shape(ctx->n_sm);
+      if (value > 0) ctx->tshape.blocks = (int)value;
+      return BGS_OK;
+    default:
+      return fail(ctx, BGS_ERR_INVALID, "unknown option %d", option);
+  }
+  return fail(ctx, BGS_ERR_INVALID, "option %d: value %g out of range", option, value);
 }
 
 int bgs_last_transport_ms(bgs_context *ctx, float *ms, uint32_t *kernel_launches) {

@@ -90,6 +90,15 @@ struct CellsDev {
   unsigned long long *off_new, *off_ce;  // exclusive prefix sums (n+1 entries)
 };
 
+// Event-mode state: per-photon carried tallies and surface, the active list
+// and the per-event queues (indices into the bank), with device counters.
+struct EventState {
+  double *thr_abs, *thr_trk;   // per-cell-visit tallies carried between stages
+  uint8_t *surface;            // face crossed by a boundary event
+  uint32_t *active, *next, *q_scatter, *q_boundary;
+  unsigned int *n_active, *n_next, *n_scatter, *n_boundary;  // device counters
+};
+
 // Scalars of one step kept on the device (so a step never waits for the host).
 struct DeviceDiag {
   double total_photon_E, emission_E, census_cell_E, source_E, pre_mat_E;

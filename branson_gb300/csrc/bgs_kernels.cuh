@@ -73,5 +73,12 @@ void launch_transport_history(const MeshDev &m, const CellsDev &c, const Bank &b
                               uint32_t seed, const TransportLaunch &shape, cudaStream_t s);
 void launch_census(const Bank &from, const Bank &to, DeviceDiag *d, const unsigned long long *off,
                    double next_dt, int n_sm, cudaStream_t s);
+void launch_transport_resume(const MeshDev &m, const CellsDev &c, const Bank &b, DeviceDiag *d,
+                             uint32_t seed, const EventState &es, const TransportLaunch &shape,
+                             cudaStream_t s);
+// event mode: one stage round (advance, scatter, boundary, rotate) per call
+void launch_event_init(const EventState &es, DeviceDiag *d, cudaStream_t s);
+void launch_event_round(const MeshDev &m, const CellsDev &c, const Bank &b, DeviceDiag *d, uint32_t seed,
+                        const EventState &es, bool first, int n_sm, cudaStream_t s);
 
 }  // namespace bgs

@@ -1,0 +1,253 @@
+// Per-segment physics of transport_photon (history_based_transport.h:55-139),
+// shared by the history kernel (bgs_transport.cu) and the event-mode stage
+// kernels (bgs_event.cu) so both run the identical arithmetic.
+#pragma once
+
+#include "bgs_fixmath.cuh"
+#include "bgs_kernels.cuh"
+
+namespace bgs {
+
+constexpr int kTransportThreads = 128;
+// Build-time choices for the per-segment arithmetic (see the header comment
+// of bgs_fixmath.cuh): integer or FP64 for the divisions, the square root
+// and sin/cos, and the minimum number of resident blocks per SM.
+#ifndef BGS_INT_DIV
+#define BGS_INT_DIV 0
+#endif
+#ifndef BGS_INT_SQRT
+#define BGS_INT_SQRT 1
+#endif
+#ifndef BGS_INT_SINCOS
+#define BGS_INT_SINCOS 1
+#endif
+#ifndef BGS_MIN_BLOCKS
+#define BGS_MIN_BLOCKS 5
+#endif
+#ifndef BGS_INT_DIV_DS
+#define BGS_INT_DIV_DS 0  // -log(u)/sigma_eff by the exact integer division (per-cell reciprocal)
+#endif
+
+__device__ __forceinline__ double seg_div(double a, double b, unsigned long long rb) {
+#if BGS_INT_DIV
+  return fix::div_rn(a, b, rb);
+#else
+  (void)rb;
+  return a / b;
+#endif
+}
+__device__ __forceinline__ double seg_sqrt(double x) {
+#if BGS_INT_SQRT
+  return fix::sqrt_rn(x);
+#else
+  return sqrt(x);
+#endif
+}
+__device__ __forceinline__ void seg_sincos(double phi, double *s, double *c) {
+#if BGS_INT_SINCOS
+  fix::sincos_phi(phi, s, c);
+#else
+  sincos(phi, s, c);
+#endif
+}
+
+struct Lane {
+  double px, py, pz, dx, dy, dz, E, E0, life, inv_E0;
+  unsigned long long rbx, rby, rbz;  // divisor reciprocals of the direction cosines
+  double n0, n1, n2, n3, n4, n5;  // nodes of the current cell
+  double thr_abs, thr_trk;
+  unsigned long long idx;
+  Rng rng;
+  uint32_t cell, group, ci, cj, ck, segs;
+};
+
+__device__ __forceinline__ void load_nodes(const MeshDev &m, Lane &L) {
+  L.n0 = m.x[L.ci]; L.n1 = m.x[L.ci + 1];
+  L.n2 = m.y[L.cj]; L.n3 = m.y[L.cj + 1];
+  L.n4 = m.z[L.ck]; L.n5 = m.z[L.ck + 1];
+}
+
+__device__ __forceinline__ void flush_tally(const CellsDev &c, const DeviceDiag *d, uint32_t cell,
+                                            double a, double t, uint32_t &flags, int sa, int st) {
+  unsigned long long lo, hi;
+  TallyCell *tc = &c.tally[cell];
+  if (a != 0.0) {
+    if (to_fixed128(a, sa, lo, hi)) atomic_add128(&tc->abs_lo, &tc->abs_hi, lo, hi);
+    else flags |= (a == a) ? FLAG_TALLY_RANGE : FLAG_NAN;
+  }
+  if (t != 0.0) {
+    if (to_fixed128(t, st, lo, hi)) atomic_add128(&tc->trk_lo, &tc->trk_hi, lo, hi);
+    else flags |= (t == t) ? FLAG_TALLY_RANGE : FLAG_NAN;
+  }
+}
+
+__device__ __forceinline__ void direction_recips(Lane &L) {
+
+#if BGS_INT_DIV
+  L.rbx = fix::divisor_recip(L.dx);
+  L.rby = fix::divisor_recip(L.dy);
+  L.rbz = fix::divisor_recip(L.dz);
+#else
+  (void)L;
+#endif
+}
+
+__device__ __forceinline__ void store_end(const Bank &b, const Lane &L, uint8_t desc) {
+  const unsigned long long i = L.idx;
+  b.px[i] = L.px; b.py[i] = L.py; b.pz[i] = L.pz;
+  b.dx[i] = L.dx; b.dy[i] = L.dy; b.dz[i] = L.dz;
+  b.E[i] = L.E; b.life[i] = L.life;
+  b.cell[i] = L.cell; b.group[i] = L.group;
+  b.desc[i] = desc; b.ctr[i] = L.rng.ctr;
+}
+
+// sample_emission_group, Cell version (sampling_functions.h:126-138) with
+// all groups at the same opacity: walk the CDF in steps of v; a walk that
+// would run past the last group stays in the last group.
+__device__ __forceinline__ uint32_t sample_group(Rng &r, double v, uint32_t n_groups) {
+  double cdf = r.next();
+  int g = -1;
+  while (cdf > 0) {
+    ++g;
+    cdf -= v;
+    if ((uint32_t)g == n_groups - 1) break;
+  }
+  return g < 0 ? 0u : (uint32_t)g;
+}
+
+
+// what one segment ends in (the event branches of transport_photon)
+enum SegEvent : int { SEG_KILLED = 0, SEG_SCATTER = 1, SEG_BOUNDARY = 2, SEG_CENSUS = 3 };
+
+// One segment up to the event decision: distance to collision, to the cell
+// faces and to census, implicit-capture decay and track tally, the move, and
+// the cutoff test (history_based_transport.h:56-91).  On SEG_KILLED the
+// remaining energy has been added to the cell's absorbed energy, as upstream.
+__device__ __forceinline__ int segment_advance(const CellXS &xs, Lane &L, uint32_t &surface_cross,
+                                               uint32_t &flags) {
+  ++L.segs;
+#if BGS_INT_DIV_DS
+  const double dist_to_scatter =
+      (xs.sig_eff > 0.0) ? fix::div_rn(fix::neg_log_u53(L.rng.next_m53()), xs.sig_eff, xs.rb_sig)
+                         : 1.0e100;
+#else
+  // -log(u) / sigma_eff with the integer, correctly rounded -log (bgs_fixmath.cuh)
+  const double dist_to_scatter =
+      (xs.sig_eff > 0.0) ? fix::neg_log_u53(L.rng.next_m53()) / xs.sig_eff : 1.0e100;
+#endif
+  // Cell::get_distance_to_boundary (cell.h:117-132)
+  double dist_to_boundary = 1.0e16;
+  surface_cross = 0;
+  const bool posx = 0.0 < L.dx, posy = 0.0 < L.dy, posz = 0.0 < L.dz;
+  {
+    double dist = seg_div((posx ? L.n1 : L.n0) - L.px, L.dx, L.rbx);
+    if (dist < dist_to_boundary) { dist_to_boundary = dist; surface_cross = posx ? 1u : 0u; }
+    dist = seg_div((posy ? L.n3 : L.n2) - L.py, L.dy, L.rby);
+    if (dist < dist_to_boundary) { dist_to_boundary = dist; surface_cross = posy ? 3u : 2u; }
+    dist = seg_div((posz ? L.n5 : L.n4) - L.pz, L.dz, L.rbz);
+    if (dist < dist_to_boundary) { dist_to_boundary = dist; surface_cross = posz ? 5u : 4u; }
+  }
+  const double dist_to_census = L.life;
+  // std::min(a, b) == (b < a) ? b : a; the event tests that follow
+  // (dist_to_event == dist_to_scatter, then == dist_to_boundary) are the
+  // same comparisons read back
+  const bool census_first = dist_to_census < dist_to_boundary;
+  const double inner = census_first ? dist_to_census : dist_to_boundary;
+  const bool inner_first = inner < dist_to_scatter;
+  const double dist_to_event = inner_first ? inner : dist_to_scatter;
+
+  const double absorbed_E = L.E * (1.0 - fix::exp_neg(-(xs.neg_saf * dist_to_event)));
+  L.thr_abs += absorbed_E;
+  L.thr_trk += absorbed_E * xs.inv_saf;
+  L.E = L.E - absorbed_E;
+  L.px += L.dx * dist_to_event;  // Photon::move (photon.h:109-114)
+  L.py += L.dy * dist_to_event;
+  L.pz += L.dz * dist_to_event;
+  L.life -= dist_to_event;
+
+  // below_cutoff: E/E0 < 0.01 (photon.h:47-49), decided from E*(1/E0) and
+  // settled with the exact quotient only within a few ulps of the threshold
+  const double frac = L.E * L.inv_E0;
+  bool killed = frac < kCutoff;
+  if (fabs(frac - kCutoff) <= 4.0e-18) killed = L.E / L.E0 < kCutoff;
+  if (killed || L.segs >= kMaxSegmentsPerHistory) {
+    if (!killed) flags |= FLAG_SEGMENT_LIMIT;
+    L.thr_abs += L.E;
+    return SEG_KILLED;
+  }
+  if (!inner_first) return SEG_SCATTER;
+  if (!census_first) return SEG_BOUNDARY;
+  return SEG_CENSUS;
+}
+
+// Effective scatter (history_based_transport.h:96-99): isotropic new
+// direction (get_uniform_angle, sampling_functions.h:57-70) and, unless
+// physical scattering wins, a resampled group.
+__device__ __forceinline__ void scatter_update(const MeshDev &m, const CellsDev &c, const CellXS &xs,
+                                               Lane &L) {
+  const double mu = mu_from_m53(L.rng.next_m53());
+  const double phi = L.rng.next() * 2.0 * kPi;
+  const double sin_theta = seg_sqrt(1.0 - mu * mu);
+  double sp, cp;
+  seg_sincos(phi, &sp, &cp);
+  L.dx = sin_theta * cp;
+  L.dy = sin_theta * sp;
+  L.dz = mu;
+  direction_recips(L);
+  // effective-scatter test and group resample (history_based_transport.h:97-98):
+  // with sigma_s = 0 the test u > 0 always passes, and with one group the
+  // walk always ends in group 0, so those draws only advance the counter
+  bool resample;
+  if (xs.p_scat > 0.0) resample = L.rng.next() > xs.p_scat;
+  else { L.rng.skip(); resample = true; }
+  if (resample) {
+    if (m.n_groups > 1) L.group = sample_group(L.rng, c.group_v[L.cell], m.n_groups);
+    else { L.rng.skip(); L.group = 0; }
+  }
+}
+
+// boundary condition of the crossed face: interior faces are ELEMENT
+// (proto_mesh.h:156-202)
+__device__ __forceinline__ int face_bc(const MeshDev &m, const Lane &L, uint32_t surface_cross) {
+  bool interior;
+  switch (surface_cross) {
+    case 0: interior = L.ci > 0; break;
+    case 1: interior = L.ci + 1 < m.ngx; break;
+    case 2: interior = L.cj > 0; break;
+    case 3: interior = L.cj + 1 < m.ngy; break;
+    case 4: interior = L.ck > 0; break;
+    default: interior = L.ck + 1 < m.ngz; break;
+  }
+  return interior ? ELEMENT : m.bc[surface_cross];
+}
+
+// ELEMENT crossing: the photon enters the neighbour (cell.h:110-112)
+__device__ __forceinline__ void enter_neighbour(const MeshDev &m, Lane &L, uint32_t surface_cross) {
+  switch (surface_cross) {
+    case 0: --L.ci; L.cell -= 1; break;
+    case 1: ++L.ci; L.cell += 1; break;
+    case 2: --L.cj; L.cell -= m.ngx; break;
+    case 3: ++L.cj; L.cell += m.ngx; break;
+    case 4: --L.ck; L.cell -= m.ngx * m.ngy; break;
+    default: ++L.ck; L.cell += m.ngx * m.ngy; break;
+  }
+  load_nodes(m, L);
+}
+
+// REFLECT: Photon::reflect (photon.h:151-155); the reciprocals depend only on
+// the magnitudes, so they are unchanged
+__device__ __forceinline__ void reflect(Lane &L, uint32_t surface_cross) {
+  if (surface_cross < 2) L.dx = -L.dx;
+  else if (surface_cross < 4) L.dy = -L.dy;
+  else L.dz = -L.dz;
+}
+
+// cell coordinates and nodes from the global cell index
+__device__ __forceinline__ void locate(const MeshDev &m, Lane &L) {
+  L.ci = L.cell % m.ngx;
+  L.cj = (L.cell / m.ngx) % m.ngy;
+  L.ck = L.cell / (m.ngx * m.ngy);
+  load_nodes(m, L);
+}
+
+}  // namespace bgs

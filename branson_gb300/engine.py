@@ -199,6 +199,10 @@ class ReplicatedIMC:
                     "bgs_replicated_transport")
         return abs_E, track_E, census.subset(int(n_c.value)), ce.value, ex.value
 
+    def set_option(self, name: str, value: float) -> None:
+        """Scheduling option (see BGS_OPT_* in the header); results do not change."""
+        self._check(self.lib.bgs_set_option(self.ctx, _lib.OPTIONS[name], float(value)), "bgs_set_option")
+
     def last_transport_ms(self):
         ms = C.c_float()
         k = C.c_uint32()

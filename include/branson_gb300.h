@@ -215,6 +215,18 @@ BGS_API int bgs_transport_device_noalloc(uint32_t ngx, uint32_t ngy, uint32_t ng
                                          const bgs_photons_host *photons, double next_dt, double *abs_E,
                                          double *track_E, void *stream);
 
+/* ---------------------------------------------------------------- tuning */
+/* Execution options (the autotuner in branson_gb300/tune.py sets these; none
+ * changes results, only how the work is scheduled).  No upstream counterpart:
+ * the reference's knobs are batch_size and n_omp_threads (input.h:249-268). */
+enum {
+  BGS_OPT_EVENT_ROUND_CAP = 0,      /* event rounds before the tail goes to the history kernel */
+  BGS_OPT_EVENT_CHECK_EVERY = 1,    /* rounds between host reads of the active count */
+  BGS_OPT_EVENT_TAIL_FRACTION = 2,  /* active share below which event rounds stop */
+  BGS_OPT_TRANSPORT_BLOCKS = 3      /* persistent-grid blocks for the history kernel (0: occupancy) */
+};
+BGS_API int bgs_set_option(bgs_context *ctx, int option, double value);
+
 /* ------------------------------------------------------- instrumentation */
 /* Device time (ms) of the last transport kernel span, measured with CUDA
  * events on the context's stream, and its launch count. */

@@ -161,3 +161,43 @@ def test_gpu_against_upstream_golden(gpu_lib, name):
             close(trk_g, cells[:, 6], CELL_RTOL, 0.0, f"{name} s{s} track_E")
             T_e = cells[:, 7]
             gpu.advance_time(nd)
+
+
+@pytest.mark.parametrize("name", ["marshak", "hot_zone", "hohlraum30"])
+def test_event_mode_reproduces_history_mode(gpu_lib, name):
+    """Event-mode stages run the same per-photon arithmetic, so end states,
+    census and tallies equal history mode bit for bit, whatever the split
+    between event rounds and the history tail."""
+    import oracle as O
+    from branson_gb300 import _lib
+    from branson_gb300.engine import ReplicatedIMC, arrays_to_records, records_to_arrays
+
+    dk = _decks()[name]
+    orc = O.Oracle(dk)
+    _, photons = orc.source(1)
+    nd = orc.next_dt()
+    with ReplicatedIMC(dk) as gpu:
+        for f in ("op_a", "op_s", "f"):
+            gpu.set_field(f, orc.arr[f])
+        ph_h = records_to_arrays(photons)
+        abs_h, trk_h, cen_h, ce_h, ex_h = gpu.replicated_transport(ph_h, nd, _lib.HISTORY)
+        for cap, tail in ((4, 0.0), (1000, 0.0), (8, 0.5)):
+            gpu.set_option("event_round_cap", cap)
+            gpu.set_option("event_tail_fraction", tail)
+            gpu.set_option("event_check_every", 2)
+            ph_e = records_to_arrays(photons)
+            abs_e, trk_e, cen_e, ce_e, ex_e = gpu.replicated_transport(ph_e, nd, _lib.EVENT)
+            for k in ph_h.arrays:
+                np.testing.assert_array_equal(ph_e[k], ph_h[k], err_msg=f"{name} cap {cap} {k}")
+            np.testing.assert_array_equal(abs_e, abs_h)
+            np.testing.assert_array_equal(trk_e, trk_h)
+            assert cen_e.n == cen_h.n and ce_e == ce_h and ex_e == ex_h
+        # and the event-mode end states are the oracle's
+        compare_photons(arrays_to_records(ph_e, O.PHOTON_DTYPE), _oracle_end(orc, photons, nd), _extent(dk),
+                        f"{name} event vs oracle")
+
+
+def _oracle_end(orc, photons, nd):
+    ph = photons.copy()
+    orc.transport(ph, nd)
+    return ph
