@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--cpu-photons", type=float, default=1e6)
+    p.add_argument("--no-adjoint", action="store_true")
+    p.add_argument("--adjoint-photons", type=float, default=1e7)
     return p.parse_args()
 
 
@@ -296,13 +298,17 @@ def run_ours(args, rank, world, local):
                "sample": f"1 step of the same deck at {int(args.cpu_photons)} photons ({h} histories), "
                          f"transport time"}
     imc.close()
+    adjoint = None
+    if not args.no_adjoint and rank == 0 and world == 1:
+        adjoint = adjoint_bench(args, dev)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": dict(cfg, parallelism=f"replicas{world}"), "roofline": roofline,
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
-                "segments_per_s": segs / elapsed * world, "histories_per_step": hist / args.steps}
+                "segments_per_s": segs / elapsed * world, "histories_per_step": hist / args.steps,
+                "adjoint": adjoint}
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -338,6 +344,104 @@ def e2e_dropin(imc, dk, args):
         + 2 * 8 * dk.n_cells
     return {"value": hist / secs, "unit": UNIT, "h2d_bytes_per_step": int(in_bytes),
             "d2h_bytes_per_step": int(out_bytes), "call": "bgs_replicated_transport", "steps": k}
+
+
+def adjoint_bench(args, dev, replicas: int = 6):
+    """Differentiation workload: 32^3 cube, one region per cell with sigma_a ~
+    lognormal(ln 20, 0.5) from seed 777, T0 = 0.1 keV, 1 keV source on x-,
+    one step of 0.01 sh at 1e7 photons; L = sum_c w_c E_abs[c] with w ~ U(0,1).
+    Reports the forward and backward call times (host wall, synchronous,
+    host arrays in and out) and their ratio.  Checks dL/dsigma_a against
+    common-random-number central differences (h = 1e-4 relative, photon
+    counts frozen) on 64 random cells among those whose absorbed-energy
+    tally has at most 1% relative statistical error.  Both estimates are
+    Monte Carlo; each is averaged over `replicas` independent-seed runs of
+    the step, and the per-cell difference is given with its standard error
+    (z) from the paired replica spread; plus the directional derivative
+    along sign(gradient) over the 64 cells."""
+    import numpy as np
+    from branson_gb300 import deck as D
+    from branson_gb300.adjoint import AdjointStep
+
+    photons = int(args.adjoint_photons)
+    dk = D.random_opacity_cube(n_per_axis=32, photons=photons, seed=777)
+    sig0 = np.array([r.opacA for r in dk.regions])[dk.cell_regions()]
+    w = np.random.default_rng(777).uniform(0.0, 1.0, dk.n_cells)
+    h = 1e-4
+    tallies, grads, tapes_info = [], [], None
+    tf, tb, fwd_kernel_ms = [], [], 0.0
+    runs = []  # per replica: (context, tape, counts)
+    for r in range(replicas):
+        dk_r = D.random_opacity_cube(n_per_axis=32, photons=photons, seed=777)
+        dk_r.seed = 777 + 1000 * r
+        st = AdjointStep(dk_r, device=dev)
+        a, tape = st.forward(sigma_a=sig0)
+        g = st.backward(tape, w)
+        if r == 0:  # timing on the first replica, after one warm-up pair
+            for _ in range(3):
+                t0 = time.perf_counter()
+                a, tape = st.forward(sigma_a=sig0, tape=tape)
+                tf.append(time.perf_counter() - t0)
+                fwd_kernel_ms, _ = st.last_transport_ms()
+                t0 = time.perf_counter()
+                g = st.backward(tape, w)
+                tb.append(time.perf_counter() - t0)
+            tapes_info = tape.info()
+        tallies.append(a)
+        grads.append(g)
+        runs.append((st, tape.counts()))
+        tape.close()
+    T = np.array(tallies)
+    mean = T.mean(axis=0)
+    rel_err = np.where(mean > 0, T.std(axis=0, ddof=1) / np.where(mean > 0, mean, 1.0), np.inf)
+    resolved = np.flatnonzero(rel_err <= 0.01)
+    rng = np.random.default_rng(4)
+    cells = rng.choice(resolved, min(64, len(resolved)), replace=False) if len(resolved) else np.array([], int)
+    G = np.array(grads)[:, cells]
+    v = np.sign(G.mean(axis=0))
+    FD, DIR_FD = [], []
+    for st, counts in runs:
+        row = []
+        for j in cells:
+            sp, sm = sig0.copy(), sig0.copy()
+            sp[j] *= 1 + h
+            sm[j] *= 1 - h
+            ap, _ = st.forward(sigma_a=sp, counts=counts, save=False)
+            am, _ = st.forward(sigma_a=sm, counts=counts, save=False)
+            row.append(float(np.dot(w, ap - am) / (2 * h * sig0[j])))
+        FD.append(row)
+        sp, sm = sig0.copy(), sig0.copy()
+        sp[cells] *= 1 + h * v
+        sm[cells] *= 1 - h * v
+        ap, _ = st.forward(sigma_a=sp, counts=counts, save=False)
+        am, _ = st.forward(sigma_a=sm, counts=counts, save=False)
+        DIR_FD.append(float(np.dot(w, ap - am) / (2 * h)))
+        st.close()
+    FD = np.array(FD)
+    diff = G - FD
+    k = len(runs)
+    rel = np.abs(diff.mean(axis=0)) / np.abs(FD.mean(axis=0))
+    se = diff.std(axis=0, ddof=1) / math.sqrt(k)
+    z = np.abs(diff.mean(axis=0)) / np.where(se > 0, se, np.inf)
+    dir_adj = (G * (sig0[cells] * v)).sum(axis=1)
+    dir_fd = np.array(DIR_FD)
+    dir_diff = dir_adj - dir_fd
+    fwd, bwd = statistics.median(tf), statistics.median(tb)
+    return {"workload": "random_opacity_cube 32^3, sigma_a ~ lognormal(ln 20, 0.5), 1 keV source on x-, "
+                        f"{photons} photons, one step of 0.01 sh",
+            "histories": int(tapes_info["n_histories"]), "segments": int(tapes_info["n_segments"]),
+            "forward_ms": 1e3 * fwd, "backward_ms": 1e3 * bwd, "backward_over_forward": bwd / fwd,
+            "forward_transport_kernel_ms": fwd_kernel_ms, "backward_replay_kernel_ms": tapes_info["replay_ms"],
+            "histories_replayed_twice": int(tapes_info["n_long"]),
+            "fd_check": {"h_rel": h, "replicas": k, "cells": int(len(cells)),
+                         "cells_with_tally_err_le_1pct": int(len(resolved)),
+                         "median_rel_diff_of_means": float(np.median(rel)) if len(rel) else None,
+                         "frac_within_1pct": float(np.mean(rel <= 0.01)) if len(rel) else None,
+                         "frac_within_3pct": float(np.mean(rel <= 0.03)) if len(rel) else None,
+                         "frac_z_le_3": float(np.mean(z <= 3.0)) if len(z) else None,
+                         "median_rel_stderr": float(np.median(se / np.abs(FD.mean(axis=0)))) if len(se) else None,
+                         "directional_rel_diff": float(abs(dir_diff.mean()) / abs(dir_fd.mean())),
+                         "directional_rel_stderr": float(dir_diff.std(ddof=1) / math.sqrt(k) / abs(dir_fd.mean()))}}
 
 
 def main():

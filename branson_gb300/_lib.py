@@ -65,6 +65,13 @@ class StepParams(C.Structure):
     _fields_ = [("step", C.c_uint32), ("algorithm", C.c_uint32), ("dt", C.c_double), ("next_dt", C.c_double)]
 
 
+class AdjointInfo(C.Structure):
+    _fields_ = [("n_histories", C.c_uint64), ("n_segments", C.c_uint64), ("n_long", C.c_uint64),
+                ("max_E", C.c_double), ("max_life", C.c_double), ("coef_max", C.c_double),
+                ("visit_bound", C.c_double), ("grad_scale", C.c_int32), ("device_flags", C.c_uint32),
+                ("replay_ms", C.c_float), ("reserved", C.c_float)]
+
+
 _lib: Optional[C.CDLL] = None
 
 # (name, restype, argtypes) of every exported entry point in include/branson_gb300.h
@@ -94,6 +101,12 @@ SIGNATURES = (
      [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
       C.POINTER(C.c_int32), C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint64,
       C.POINTER(PhotonsHost), C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("bgs_adjoint_forward", C.c_int,
+     [C.c_void_p, C.POINTER(StepParams), C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
+    ("bgs_adjoint_backward", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("bgs_adjoint_counts", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("bgs_adjoint_get_info", C.c_int, [C.c_void_p, C.POINTER(AdjointInfo)]),
+    ("bgs_adjoint_release", C.c_int, [C.c_void_p]),
     ("bgs_set_option", C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     ("bgs_last_transport_ms", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_uint32)]),
     ("bgs_kernel_launch_count", C.c_uint64, [C.c_void_p]),

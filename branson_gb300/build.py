@@ -18,7 +18,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libbranson_gb300.so")
-SOURCES = ("bgs_api.cu", "bgs_mesh.cu", "bgs_source.cu", "bgs_transport.cu", "bgs_event.cu", "bgs_noalloc.cu")
+SOURCES = ("bgs_api.cu", "bgs_mesh.cu", "bgs_source.cu", "bgs_transport.cu", "bgs_event.cu", "bgs_noalloc.cu",
+           "bgs_adjoint.cu", "bgs_adjoint_api.cu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-fvisibility=hidden", "--expt-relaxed-constexpr",

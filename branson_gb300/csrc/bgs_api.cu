@@ -2,127 +2,12 @@
 // lifetime, device memory, the staged step and the host-buffer drop-in for
 // replicated_transport.  Host-side orchestration only; all arithmetic runs
 // in the kernels of bgs_mesh.cu, bgs_source.cu and bgs_transport.cu.
-#include <cstdarg>
-#include <cstdio>
 #include <cstring>
 #include <new>
-#include <string>
-#include <vector>
 
-#include "../../include/branson_gb300.h"
-#include "bgs_kernels.cuh"
-
-using namespace bgs;
-
-struct bgs_context {
-  int device = 0;
-  int n_sm = 0;
-  cudaStream_t stream = nullptr;
-  bool own_stream = false;
-  uint32_t seed = 0;
-  unsigned long long n_user = 0;
-  unsigned long long capacity = 0;
-  bool has_mesh = false;
-  bool xs_dirty = true;
-
-  MeshDev mesh{};
-  CellsDev cells{};
-  std::vector<void *> mesh_allocs;  // freed on set_mesh / destroy
-  double *d_mat_E = nullptr, *d_abs = nullptr, *d_track = nullptr, *d_mat_part = nullptr;
-  double *d_energy_part = nullptr;
-  unsigned long long *d_tile_cells = nullptr;
-
-  Bank bank[2]{};
-  int cur = 0;
-  std::vector<void *> bank_allocs;
-  unsigned long long *d_off_bank = nullptr, *d_tile_bank = nullptr, *d_maxbits = nullptr;
-
-  // event mode (allocated on first use): carried tallies, surfaces, lists, counters
-  std::vector<void *> event_allocs;
-  EventState ev_a{}, ev_b{};     // ev_b has active/next swapped
-  unsigned int *h_counter = nullptr;  // pinned
-  uint32_t event_round_cap = 64;      // rounds before the tail goes to the history kernel
-  uint32_t event_check_every = 4;     // rounds between host reads of the active count
-  double event_tail_fraction = 0.02;  // active share below which the tail goes to history mode
-  unsigned long long last_event_rounds = 0;
-
-  DeviceDiag *d_diag = nullptr;
-  DeviceDiag *h_diag = nullptr;  // pinned
-  TransportLaunch tshape{};
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  uint32_t last_launches = 0;
-  unsigned long long launches = 0;
-  bool bank_is_census = true;  // current bank holds a census (after transport)
-  std::string err;
-};
+#include "bgs_context.cuh"
 
 namespace {
-
-int fail(bgs_context *ctx, int code, const char *fmt, ...) {
-  char buf[512];
-  va_list ap;
-  va_start(ap, fmt);
-  vsnprintf(buf, sizeof(buf), fmt, ap);
-  va_end(ap);
-  if (ctx) ctx->err = buf;
-  return code;
-}
-
-#define BGS_CUDA(ctx, call)                                                                   \
-  do {                                                                                        \
-    cudaError_t e_ = (call);                                                                  \
-    if (e_ != cudaSuccess)                                                                    \
-      return fail((ctx), BGS_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));       \
-  } while (0)
-
-#define BGS_LAUNCHED(ctx, n)                                                                  \
-  do {                                                                                        \
-    cudaError_t e_ = cudaGetLastError();                                                      \
-    if (e_ != cudaSuccess)                                                                    \
-      return fail((ctx), BGS_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e_));   \
-    (ctx)->launches += (n);                                                                   \
-  } while (0)
-
-template <typename T>
-int dev_alloc(bgs_context *ctx, std::vector<void *> &list, T **p, size_t count) {
-  void *q = nullptr;
-  const size_t bytes = count * sizeof(T) > 0 ? count * sizeof(T) : 16;
-  cudaError_t e = cudaMalloc(&q, bytes);
-  if (e != cudaSuccess)
-    return fail(ctx, BGS_ERR_CUDA, "cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
-  list.push_back(q);
-  *p = static_cast<T *>(q);
-  return BGS_OK;
-}
-
-void free_list(std::vector<void *> &list) {
-  for (void *p : list) cudaFree(p);
-  list.clear();
-}
-
-int set_device(bgs_context *ctx) {
-  BGS_CUDA(ctx, cudaSetDevice(ctx->device));
-  return BGS_OK;
-}
-
-int check_flags(bgs_context *ctx, uint32_t flags) {
-  if (!flags) return BGS_OK;
-  std::string what;
-  if (flags & FLAG_CAPACITY) what += " photon-bank capacity exceeded (no photons made);";
-  if (flags & FLAG_TALLY_RANGE) what += " tally contribution outside the fixed-point range;";
-  if (flags & FLAG_SEGMENT_LIMIT) what += " a history hit the segment limit;";
-  if (flags & FLAG_BAD_CELL) what += " a photon referenced a cell outside the mesh;";
-  if (flags & FLAG_NAN) what += " a non-finite tally contribution was dropped;";
-  return fail(ctx, (flags & FLAG_CAPACITY) ? BGS_ERR_CAPACITY : BGS_ERR_DEVICE,
-              "device check fired (flags 0x%x):%s", flags, what.c_str());
-}
-
-int read_diag(bgs_context *ctx) {
-  BGS_CUDA(ctx, cudaMemcpyAsync(ctx->h_diag, ctx->d_diag, sizeof(DeviceDiag), cudaMemcpyDeviceToHost,
-                                ctx->stream));
-  BGS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  return BGS_OK;
-}
 
 void fill_transport_diag(const DeviceDiag &d, bgs_transport_diag *out) {
   out->n_transported = d.n_bank;
@@ -292,6 +177,7 @@ int bgs_destroy(bgs_context *ctx) {
   free_list(ctx->mesh_allocs);
   free_list(ctx->bank_allocs);
   free_list(ctx->event_allocs);
+  free_list(ctx->adj_allocs);
   if (ctx->h_counter) cudaFreeHost(ctx->h_counter);
   if (ctx->d_diag) cudaFree(ctx->d_diag);
   if (ctx->h_diag) cudaFreeHost(ctx->h_diag);
@@ -372,6 +258,7 @@ int bgs_set_mesh(bgs_context *ctx, const bgs_mesh_desc *md) {
   BGS_CUDA(ctx, cudaMemsetAsync(ctx->d_diag, 0, sizeof(DeviceDiag), ctx->stream));
   BGS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   ctx->has_mesh = true;
+  ++ctx->mesh_generation;
   ctx->xs_dirty = true;
   ctx->bank_is_census = true;
   return BGS_OK;
@@ -451,7 +338,11 @@ int bgs_source(bgs_context *ctx, uint32_t step, double dt) {
   return BGS_OK;
 }
 
-static int ensure_event_state(bgs_context *ctx) {
+}  // extern "C"
+
+namespace {
+
+int ensure_event_state(bgs_context *ctx) {
   if (ctx->ev_a.active) return BGS_OK;
   const unsigned long long cap = ctx->capacity;
   EventState e{};
@@ -476,7 +367,7 @@ static int ensure_event_state(bgs_context *ctx) {
 
 // Event mode: stage rounds while the active set is large, then the history
 // kernel finishes the tail from the carried state.
-static int transport_event(bgs_context *ctx, const Bank &from) {
+int transport_event(bgs_context *ctx, const Bank &from) {
   int rc;
   if ((rc = ensure_event_state(ctx))) return rc;
   launch_event_init(ctx->ev_a, ctx->d_diag, ctx->stream);
@@ -516,7 +407,9 @@ static int transport_event(bgs_context *ctx, const Bank &from) {
   return BGS_OK;
 }
 
-static int transport_impl(bgs_context *ctx, double next_dt, uint32_t algorithm, bool read_back) {
+}  // namespace
+
+int run_transport(bgs_context *ctx, const Bank &from, uint32_t algorithm) {
   if (algorithm != BGS_HISTORY && algorithm != BGS_EVENT)
     return fail(ctx, BGS_ERR_INVALID, "unknown transport algorithm %u", algorithm);
   if (ctx->xs_dirty) {
@@ -524,9 +417,6 @@ static int transport_impl(bgs_context *ctx, double next_dt, uint32_t algorithm, 
     BGS_LAUNCHED(ctx, 1);
     ctx->xs_dirty = false;
   }
-  const uint64_t before = ctx->launches;
-  Bank &from = ctx->bank[ctx->cur];
-  Bank &to = ctx->bank[1 - ctx->cur];
   launch_bank_bounds(from, ctx->d_maxbits, ctx->d_diag, ctx->n_sm, ctx->stream);
   BGS_LAUNCHED(ctx, 2);
   BGS_CUDA(ctx, cudaMemsetAsync(ctx->cells.tally, 0, ctx->mesh.n_cells * sizeof(TallyCell), ctx->stream));
@@ -541,6 +431,17 @@ static int transport_impl(bgs_context *ctx, double next_dt, uint32_t algorithm, 
     BGS_LAUNCHED(ctx, 1);
   }
   BGS_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+  return BGS_OK;
+}
+
+namespace {
+
+int transport_impl(bgs_context *ctx, double next_dt, uint32_t algorithm) {
+  const uint64_t before = ctx->launches;
+  Bank &from = ctx->bank[ctx->cur];
+  Bank &to = ctx->bank[1 - ctx->cur];
+  int rc;
+  if ((rc = run_transport(ctx, from, algorithm))) return rc;
   launch_scan_flags(from.desc, CENSUS, (uint32_t)ctx->capacity, &ctx->d_diag->n_bank, ctx->d_off_bank,
                     ctx->d_tile_bank, ctx->stream);
   BGS_LAUNCHED(ctx, 3);
@@ -551,16 +452,19 @@ static int transport_impl(bgs_context *ctx, double next_dt, uint32_t algorithm, 
   ctx->last_launches = (uint32_t)(ctx->launches - before);
   ctx->cur = 1 - ctx->cur;
   ctx->bank_is_census = true;
-  (void)read_back;
   return BGS_OK;
 }
+
+}  // namespace
+
+extern "C" {
 
 int bgs_transport(bgs_context *ctx, double next_dt, uint32_t algorithm, bgs_transport_diag *out) {
   if (!ctx) return BGS_ERR_INVALID;
   if (!ctx->has_mesh) return fail(ctx, BGS_ERR_STATE, "no mesh");
   int rc = set_device(ctx);
   if (rc) return rc;
-  if ((rc = transport_impl(ctx, next_dt, algorithm, out != nullptr))) return rc;
+  if ((rc = transport_impl(ctx, next_dt, algorithm))) return rc;
   if (out) {
     if ((rc = read_diag(ctx))) return rc;
     fill_transport_diag(*ctx->h_diag, out);
@@ -590,7 +494,7 @@ int bgs_step(bgs_context *ctx, const bgs_step_params *p, bgs_transport_diag *out
   int rc;
   if ((rc = bgs_calculate_photon_energy(ctx, p->step, p->dt, nullptr))) return rc;
   if ((rc = bgs_source(ctx, p->step, p->dt))) return rc;
-  if ((rc = transport_impl(ctx, p->next_dt, p->algorithm, out != nullptr))) return rc;
+  if ((rc = transport_impl(ctx, p->next_dt, p->algorithm))) return rc;
   if ((rc = bgs_update_temperature(ctx, p->dt, out))) return rc;
   return BGS_OK;
 }
@@ -655,7 +559,7 @@ int bgs_replicated_transport(bgs_context *ctx, uint64_t n, const bgs_photons_hos
   if (!ctx->has_mesh) return fail(ctx, BGS_ERR_STATE, "no mesh");
   int rc;
   if ((rc = bgs_set_photons(ctx, n, photons))) return rc;
-  if ((rc = transport_impl(ctx, next_dt, algorithm, true))) return rc;
+  if ((rc = transport_impl(ctx, next_dt, algorithm))) return rc;
   // end states come back from the bank that was transported
   const Bank &done = ctx->bank[1 - ctx->cur];
   bgs_photons_host back = *photons;

@@ -34,6 +34,7 @@ enum : uint32_t {
   FLAG_SEGMENT_LIMIT = 1u << 2, // a history exceeded the segment limit and was killed
   FLAG_BAD_CELL = 1u << 3,      // a photon referenced a cell outside the mesh
   FLAG_NAN = 1u << 4,           // a non-finite tally contribution was dropped
+  FLAG_BAD_COUNTS = 1u << 5,    // caller-supplied photon counts disagree with the cell energies
 };
 
 // Upper bound on loop trips of one history inside one step; a history that
@@ -97,6 +98,30 @@ struct EventState {
   uint8_t *surface;            // face crossed by a boundary event
   uint32_t *active, *next, *q_scatter, *q_boundary;
   unsigned int *n_active, *n_next, *n_scatter, *n_boundary;  // device counters
+};
+
+// Adjoint replay (bgs_adjoint.cu).  Per cell: w = dL/dE_abs of the cell,
+// f2 = f^2 = d(sigma_a f)/d sigma_a, g2 = 1 - f^2 = d sigma_eff/d sigma_a, and
+// inv_se = 1/sigma_eff (0 when sigma_eff is 0).
+struct __align__(32) AdjCell {
+  double w, f2, g2, inv_se;
+};
+
+struct AdjointDev {
+  const AdjCell *cell;
+  const double *src;              // f/sigma_a: d ln(emission weight)/d sigma_a per cell
+  unsigned long long *grad;       // per cell (lo, hi): 128-bit two's-complement fixed point
+  double *log_a, *log_b;          // per-thread visit logs, log_len entries each
+  uint32_t *log_cell;
+  uint32_t *long_list;            // histories with more visits than a log holds
+  double *long_G;                 // their totals (second replay)
+  unsigned int *n_long;
+  unsigned long long *work;       // work-queue head
+  uint32_t *flags;
+  unsigned long long n;           // histories on the tape
+  double visit_bound;             // |contribution of one visit| above this is a range error
+  int scale;                      // fixed-point exponent of the gradient sums
+  uint32_t log_len;
 };
 
 // Scalars of one step kept on the device (so a step never waits for the host).
@@ -218,6 +243,17 @@ __device__ __forceinline__ void atomic_add128(unsigned long long *lo_p, unsigned
   if (hi) atomicAdd(hi_p, hi);
 }
 
+// signed values in two's complement: |x| as above, negated if x < 0
+__device__ __forceinline__ bool to_fixed128_signed(double x, int scale, unsigned long long &lo,
+                                                   unsigned long long &hi) {
+  const bool ok = to_fixed128(fabs(x), scale, lo, hi);
+  if (x < 0.0) {
+    lo = ~lo + 1ULL;
+    hi = ~hi + (lo == 0ULL ? 1ULL : 0ULL);
+  }
+  return ok;
+}
+
 __host__ __device__ __forceinline__ double from_fixed128(unsigned long long lo, unsigned long long hi,
                                                          int scale) {
   const double v = (double)hi * 18446744073709551616.0 + (double)lo;
@@ -226,6 +262,14 @@ __host__ __device__ __forceinline__ double from_fixed128(unsigned long long lo, 
 #else
   return __builtin_scalbn(v, -scale);
 #endif
+}
+
+__host__ __device__ __forceinline__ double from_fixed128_signed(unsigned long long lo, unsigned long long hi,
+                                                                int scale) {
+  if (!(hi >> 63)) return from_fixed128(lo, hi, scale);
+  const unsigned long long nlo = ~lo + 1ULL;
+  const unsigned long long nhi = ~hi + (nlo == 0ULL ? 1ULL : 0ULL);
+  return -from_fixed128(nlo, nhi, scale);
 }
 
 // exponent such that bound * 2^scale <= 2^118 (ten bits of headroom below 2^128)

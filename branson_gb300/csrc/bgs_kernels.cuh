@@ -43,7 +43,9 @@ __device__ __forceinline__ void set_cell_xs(const CellsDev &c, uint32_t g, doubl
 void launch_init_cells(const MeshDev &m, const CellsDev &c, cudaStream_t s);
 uint32_t energy_parts(uint32_t n_cells);
 void launch_cell_energy(const MeshDev &m, const CellsDev &c, uint32_t step, double dt, double *mat_E,
-                        double *part, DeviceDiag *d, unsigned long long n_user, cudaStream_t s);
+                        double *part, DeviceDiag *d, unsigned long long n_user, cudaStream_t s,
+                        const double *op_a_in = nullptr);
+void launch_check_counts(const MeshDev &m, const CellsDev &c, DeviceDiag *d, uint32_t step, cudaStream_t s);
 void launch_cell_xs(const MeshDev &m, const CellsDev &c, cudaStream_t s);
 uint32_t scan_tiles_needed(uint64_t n);
 void launch_scan_counts(const uint32_t *cnt, const uint32_t *cnt2, uint32_t n,
@@ -80,5 +82,15 @@ void launch_transport_resume(const MeshDev &m, const CellsDev &c, const Bank &b,
 void launch_event_init(const EventState &es, DeviceDiag *d, cudaStream_t s);
 void launch_event_round(const MeshDev &m, const CellsDev &c, const Bank &b, DeviceDiag *d, uint32_t seed,
                         const EventState &es, bool first, int n_sm, cudaStream_t s);
+
+// adjoint replay of a saved photon bank (bgs_adjoint.cu)
+TransportLaunch adjoint_launch_shape(int n_sm);
+void launch_adjoint_cells(const CellsDev &c, uint32_t n_cells, AdjCell *adj, double *src,
+                          unsigned long long *coef_max_bits, cudaStream_t s);
+void launch_adjoint_set_w(uint32_t n_cells, AdjCell *adj, const double *w, cudaStream_t s);
+void launch_adjoint_replay(const MeshDev &m, const CellsDev &c, const Bank &tape, const AdjointDev &a,
+                           uint32_t seed, const TransportLaunch &shape, cudaStream_t s);
+void launch_adjoint_grad_to_double(uint32_t n_cells, const unsigned long long *grad, int scale, double *out,
+                                   cudaStream_t s);
 
 }  // namespace bgs

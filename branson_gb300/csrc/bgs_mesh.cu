@@ -40,7 +40,8 @@ __device__ __forceinline__ double face_area(const double n[6], int face) {
 
 // Mesh::calculate_photon_energy per cell (mesh.h:253-287), one rank
 // (replicated factor 1).  Also derives the transport table.
-__global__ void k_cell_energy(MeshDev m, CellsDev c, uint32_t step, double dt, double *mat_E) {
+__global__ void k_cell_energy(MeshDev m, CellsDev c, uint32_t step, double dt, double *mat_E,
+                              const double *op_a_in) {
   const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= m.n_cells) return;
   double n[6];
@@ -50,7 +51,9 @@ __global__ void k_cell_energy(MeshDev m, CellsDev c, uint32_t step, double dt, d
   const double cV = r[0], rho = r[1], A = r[2], B = r[3], Cx = r[4], S = r[5];
   const double T = c.T_e[g], Tr = c.T_r[g], Ts = c.T_s[g];
   const double rf = 1.0;
-  const double op_a = A + B * pow(T, Cx);
+  // Region::get_absorption_opacity (region.h:44-46), or the caller's
+  // per-cell opacity when it supplies one (the adjoint forward)
+  const double op_a = op_a_in ? op_a_in[g] : A + B * pow(T, Cx);
   const double op_s = S;
   const double f = 1.0 / (1.0 + dt * op_a * kC * (4.0 * kA * pow(T, 3.0) / (cV * rho)));
   c.op_a[g] = op_a;
@@ -171,6 +174,21 @@ __global__ void k_counts(MeshDev m, CellsDev c, const DeviceDiag *d, unsigned lo
   c.n_em[g] = photons_for(n_user, c.em_E[g], total);
   c.n_so[g] = photons_for(n_user, c.so_E[g], total);
   c.n_ce[g] = step == 1 ? photons_for(n_user, c.ce_E[g], total) : 0u;
+}
+
+// counts supplied by the caller (frozen across perturbed runs) must give every
+// cell with energy at least one photon and none to a cell without
+__global__ void k_check_counts(MeshDev m, CellsDev c, DeviceDiag *d, uint32_t step) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= m.n_cells) return;
+  bool bad = (c.em_E[g] > 0.0) != (c.n_em[g] > 0u) || (c.so_E[g] > 0.0) != (c.n_so[g] > 0u);
+  if (step == 1) bad |= (c.ce_E[g] > 0.0) != (c.n_ce[g] > 0u);
+  else bad |= c.n_ce[g] != 0u;
+  if (bad) atomicOr(&d->flags, (uint32_t)FLAG_BAD_COUNTS);
+}
+
+void launch_check_counts(const MeshDev &m, const CellsDev &c, DeviceDiag *d, uint32_t step, cudaStream_t s) {
+  k_check_counts<<<(m.n_cells + 255) / 256, 256, 0, s>>>(m, c, d, step);
 }
 
 // ---------------------------------------------------------------------------
@@ -436,10 +454,11 @@ void launch_init_cells(const MeshDev &m, const CellsDev &c, cudaStream_t s) {
 uint32_t energy_parts(uint32_t n_cells) { return (n_cells + kSumThreads - 1) / kSumThreads; }
 
 void launch_cell_energy(const MeshDev &m, const CellsDev &c, uint32_t step, double dt, double *mat_E,
-                        double *part, DeviceDiag *d, unsigned long long n_user, cudaStream_t s) {
+                        double *part, DeviceDiag *d, unsigned long long n_user, cudaStream_t s,
+                        const double *op_a_in) {
   const uint32_t blocks = (m.n_cells + 255) / 256;
   const uint32_t parts = energy_parts(m.n_cells);
-  k_cell_energy<<<blocks, 256, 0, s>>>(m, c, step, dt, mat_E);
+  k_cell_energy<<<blocks, 256, 0, s>>>(m, c, step, dt, mat_E, op_a_in);
   k_energy_partials<<<parts, kSumThreads, 0, s>>>(m, c, mat_E, part);
   k_energy_finish<<<1, 32, 0, s>>>(part, parts, d);
   k_energy_check<<<blocks, 256, 0, s>>>(m, c, d, n_user, step);

@@ -119,12 +119,20 @@ __device__ __forceinline__ uint32_t sample_group(Rng &r, double v, uint32_t n_gr
 // what one segment ends in (the event branches of transport_photon)
 enum SegEvent : int { SEG_KILLED = 0, SEG_SCATTER = 1, SEG_BOUNDARY = 2, SEG_CENSUS = 3 };
 
+// details of a segment the adjoint replay needs (unused elsewhere, so the
+// compiler drops them from the other kernels)
+struct SegInfo {
+  double d;          // distance moved
+  double absorbed;   // energy absorbed on the way
+  bool collided;     // the segment ended at the sampled collision distance
+};
+
 // One segment up to the event decision: distance to collision, to the cell
 // faces and to census, implicit-capture decay and track tally, the move, and
 // the cutoff test (history_based_transport.h:56-91).  On SEG_KILLED the
 // remaining energy has been added to the cell's absorbed energy, as upstream.
 __device__ __forceinline__ int segment_advance(const CellXS &xs, Lane &L, uint32_t &surface_cross,
-                                               uint32_t &flags) {
+                                               uint32_t &flags, SegInfo *info = nullptr) {
   ++L.segs;
 #if BGS_INT_DIV_DS
   const double dist_to_scatter =
@@ -164,6 +172,11 @@ __device__ __forceinline__ int segment_advance(const CellXS &xs, Lane &L, uint32
   L.py += L.dy * dist_to_event;
   L.pz += L.dz * dist_to_event;
   L.life -= dist_to_event;
+  if (info) {
+    info->d = dist_to_event;
+    info->absorbed = absorbed_E;
+    info->collided = !inner_first;
+  }
 
   // below_cutoff: E/E0 < 0.01 (photon.h:47-49), decided from E*(1/E0) and
   // settled with the exact quotient only within a few ulps of the threshold

@@ -215,6 +215,60 @@ BGS_API int bgs_transport_device_noalloc(uint32_t ngx, uint32_t ngy, uint32_t ng
                                          const bgs_photons_host *photons, double next_dt, double *abs_E,
                                          double *track_E, void *stream);
 
+/* ------------------------------------------------------------- adjoint */
+/* No counterpart in the reference, which computes no derivatives.  An
+ * autograd-style pair for L = sum_c w_c E_abs[c], any weighted sum of one
+ * step's absorbed-energy tally, differentiated with respect to each cell's
+ * absorption opacity sigma_a (the Fleck factor f = 1/(1 + K sigma_a) of
+ * mesh.h:267 and the emission energy dt V f sigma_a a c T^4 of mesh.h:272
+ * follow sigma_a; photon counts are held at the forward's values).
+ *
+ * bgs_adjoint_forward: one step's energies (calculate_photon_energy with the
+ *   caller's sigma_a per cell in place of the region law when sigma_a is not
+ *   NULL), photon counts (the caller's when counts is not NULL: 3*n_cells
+ *   values, emission | boundary source | initial census, e.g. from
+ *   bgs_adjoint_counts of an earlier forward, so that perturbed runs use
+ *   the same photons and random streams), sourcing and history/event
+ *   transport; abs_E (host, n_cells) receives the tally.  The context's
+ *   bank keeps the step's start states (the transport runs on a copy), its
+ *   cell fields hold this step's opacities, Fleck factors and energies, and
+ *   its step counter does not move, so repeated forwards at the same step
+ *   see the same census.  With tape != NULL the start states and the step's
+ *   cell coefficients are saved: *tape == NULL makes a new tape, an existing
+ *   tape is reused (its memory grows if needed).
+ * bgs_adjoint_backward: grad_abs_E = dL/dE_abs (host, n_cells) in,
+ *   grad_sigma_a = dL/dsigma_a (host, n_cells) out.  Replays every saved
+ *   history from its start state and random-number counter (nothing per
+ *   segment is stored by the forward): pathwise derivatives of the weight
+ *   decay exp(-sigma_a f d) and of f, a score-function term for the
+ *   sampling of effective-scatter collision distances, and the emission
+ *   weight term; sums are exact 128-bit fixed point.  A tape can be
+ *   backpropagated any number of times, with any weights, while the
+ *   context's mesh is unchanged.
+ * bgs_adjoint_counts: the forward's photon counts (3*n_cells values). */
+typedef struct bgs_adjoint_tape bgs_adjoint_tape;
+
+typedef struct {
+  uint64_t n_histories;      /* photons the forward transported and saved */
+  uint64_t n_segments;       /* their history-loop trips */
+  uint64_t n_long;           /* last backward: histories replayed twice (long visit lists) */
+  double max_E, max_life;    /* largest starting weight and flight length on the tape */
+  double coef_max;           /* largest per-cell f/sigma_a or (1-f^2)/sigma_eff */
+  double visit_bound;        /* last backward: range of one cell visit's contribution */
+  int32_t grad_scale;        /* last backward: fixed-point exponent of the sums */
+  uint32_t device_flags;     /* last backward: device checks that fired */
+  float replay_ms;           /* last backward: device time of the replay kernels */
+  float reserved;
+} bgs_adjoint_info;
+
+BGS_API int bgs_adjoint_forward(bgs_context *ctx, const bgs_step_params *p, const double *sigma_a,
+                                const uint32_t *counts, double *abs_E, bgs_adjoint_tape **tape);
+BGS_API int bgs_adjoint_backward(bgs_context *ctx, bgs_adjoint_tape *tape, const double *grad_abs_E,
+                                 double *grad_sigma_a);
+BGS_API int bgs_adjoint_counts(const bgs_adjoint_tape *tape, uint32_t *counts);
+BGS_API int bgs_adjoint_get_info(const bgs_adjoint_tape *tape, bgs_adjoint_info *info);
+BGS_API int bgs_adjoint_release(bgs_adjoint_tape *tape);
+
 /* ---------------------------------------------------------------- tuning */
 /* Execution options (the autotuner in branson_gb300/tune.py sets these; none
  * changes results, only how the work is scheduled).  No upstream counterpart:

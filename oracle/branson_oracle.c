@@ -620,3 +620,270 @@ void bo_update_temperature(const bo_mesh *m, bo_cells *c, double dt, double *abs
   *total_abs_E = tot_abs;
   *post_mat_E = tot_mat;
 }
+
+/* ------------------------------------------------------------------ adjoint
+ * CPU replay of the GPU adjoint estimator (no upstream counterpart; the
+ * estimator is documented in branson_gb300/csrc/bgs_adjoint.cu).  Each
+ * history is walked with the statements of transport_photon above, so the
+ * path is the forward one; per segment in cell j with length d:
+ *   s = 1/sigma_eff - d (ended at the collision distance) or -d,
+ *   A += (1-f^2) s - f^2 d,
+ *   B += (1-f^2) s prefix_before - f^2 d (prefix_after + w_j W_after),
+ * per cell visit G*A - B is added to the cell, and an emission photon adds
+ * G f/sigma_a to its birth cell; G is the history's weighted deposit.  Sums
+ * are 128-bit two's-complement fixed point with the truncating conversion
+ * of the device code, so both give the same bits for the same histories. */
+typedef struct {
+  double f2, g2, inv_se, src;
+} bo_adj_coef;
+
+typedef struct {
+  uint32_t cell;
+  double a, b;
+} bo_visit;
+
+typedef struct {
+  bo_visit *v;
+  size_t n, cap;
+} bo_visit_log;
+
+static void visit_push(bo_visit_log *L, uint32_t cell, double a, double b) {
+  if (L->n == L->cap) {
+    L->cap = L->cap ? 2 * L->cap : 64;
+    L->v = (bo_visit *)realloc(L->v, L->cap * sizeof(bo_visit));
+  }
+  L->v[L->n].cell = cell;
+  L->v[L->n].a = a;
+  L->v[L->n].b = b;
+  ++L->n;
+}
+
+/* floor(|x| * 2^scale) as a 128-bit integer, negated for x < 0; 0 if out of
+ * range (the caller checks the range first) */
+static unsigned __int128 fixed128_signed(double x, int scale) {
+  const double ax = fabs(x);
+  uint64_t bits;
+  memcpy(&bits, &ax, sizeof(bits));
+  const int e = (int)((bits >> 52) & 0x7FF);
+  unsigned __int128 v = 0;
+  if (e != 0 && e != 0x7FF) {
+    const uint64_t mant = (bits & 0x000FFFFFFFFFFFFFULL) | 0x0010000000000000ULL;
+    const int sh = e - 1075 + scale;
+    if (sh >= 0) {
+      if (sh <= 74) v = (unsigned __int128)mant << sh;
+    } else if (sh > -64) {
+      v = (unsigned __int128)(mant >> (-sh));
+    }
+  }
+  return x < 0.0 ? (unsigned __int128)0 - v : v;
+}
+
+static double fixed128_to_double(unsigned __int128 v, int scale) {
+  const int neg = (int)(v >> 127);
+  if (neg) v = (unsigned __int128)0 - v;
+  const uint64_t hi = (uint64_t)(v >> 64), lo = (uint64_t)v;
+  const double d = (double)hi * 18446744073709551616.0 + (double)lo;
+  const double r = scalbn(d, -scale);
+  return neg ? -r : r;
+}
+
+/* One history replayed from its start state.  Fills `log` with its cell
+ * visits (A, B) and returns G.  With op_a_p/f_p (perturbed opacities and
+ * Fleck factors) it also returns, in *L_rw, the history's contribution to
+ * L at the perturbed opacities estimated on this same path: weights decay
+ * with the perturbed sigma_a f, an emission weight scales with f sigma_a,
+ * and each deposit is multiplied by the likelihood ratio of the path's
+ * segment lengths up to it (sigma_eff' exp(-sigma_eff' d) over sigma_eff
+ * exp(-sigma_eff d) for collisions, exp(-(sigma_eff' - sigma_eff) d)
+ * otherwise).  Its derivative at the unperturbed values is this history's
+ * estimator term. */
+static double adjoint_replay_photon(const bo_mesh *m, const bo_cells *c, const bo_adj_coef *k,
+                                    uint32_t seed, const bo_photon *start, const double *w,
+                                    bo_visit_log *visits, const double *op_a_p, const double *f_p,
+                                    double *L_rw) {
+  bo_photon ph = *start;
+  bo_photon *p = &ph;
+  bo_rng r;
+  rng_init(&r, seed, p->stream, p->counter);
+  uint32_t surface_cross = 0;
+  uint32_t cell = p->cell;
+  const uint32_t sxy = m->ngx * m->ngy;
+  uint32_t ci = cell % m->ngx, cj = (cell / m->ngx) % m->ngy, ck = cell / sxy;
+  double nodes[6] = {m->x[ci], m->x[ci + 1], m->y[cj], m->y[cj + 1], m->z[ck], m->z[ck + 1]};
+  double prefix = 0.0, vis_a = 0.0, vis_b = 0.0;
+  double W_rw = p->E, lr = 1.0, acc_rw = 0.0;
+  visits->n = 0;
+  if (p->source_type == 2) { /* emission: weight proportional to f sigma_a of the birth cell */
+    visit_push(visits, cell, k[cell].src, 0.0);
+    if (op_a_p) W_rw = p->E * ((f_p[cell] * op_a_p[cell]) / (c->f[cell] * c->op_a[cell]));
+  }
+  int active = 1;
+  while (active) {
+    const double sigma_s = c->op_s[cell];
+    const double sigma_a = c->op_a[cell];
+    const double f = c->f[cell];
+    const double total_sigma_s = (1.0 - f) * sigma_a + sigma_s;
+    const double dist_to_scatter =
+        (total_sigma_s > 0.0) ? -log(rng_next(&r)) / total_sigma_s : 1.0e100;
+    const double dist_to_boundary = distance_to_boundary(nodes, p->pos, p->dir, &surface_cross);
+    const double dist_to_census = p->life_dx;
+    const double db_dc = (dist_to_census < dist_to_boundary) ? dist_to_census : dist_to_boundary;
+    const double dist_to_event = (db_dc < dist_to_scatter) ? db_dc : dist_to_scatter;
+    const double absorbed_E = p->E * (1.0 - exp(-sigma_a * f * dist_to_event));
+    p->E = p->E - absorbed_E;
+    p->pos[0] += p->dir[0] * dist_to_event;
+    p->pos[1] += p->dir[1] * dist_to_event;
+    p->pos[2] += p->dir[2] * dist_to_event;
+    p->life_dx -= dist_to_event;
+    const int collided = !(db_dc < dist_to_scatter);
+    const int killed = p->E / p->E0 < BO_CUTOFF;
+    { /* estimator terms of this segment */
+      const bo_adj_coef a = k[cell];
+      const double wj = w[cell];
+      const double d = dist_to_event;
+      const double s = collided ? a.inv_se - d : -d;
+      const double gs = a.g2 * s;
+      const double pa = a.f2 * d;
+      const double prev = prefix;
+      prefix = prefix + wj * absorbed_E;
+      const double tail = prefix + wj * p->E;
+      vis_a = vis_a + (gs - pa);
+      vis_b = vis_b + (gs * prev - pa * tail);
+      if (killed) prefix = tail;
+      if (op_a_p) {
+        const double sp = op_a_p[cell], fp = f_p[cell];
+        const double se_p = (1.0 - fp) * sp + sigma_s;
+        lr *= exp(-(se_p - total_sigma_s) * d);
+        if (collided) lr *= se_p / total_sigma_s;
+        const double dep = W_rw * (1.0 - exp(-sp * fp * d));
+        W_rw -= dep;
+        acc_rw += wj * dep * lr;
+        if (killed) acc_rw += wj * W_rw * lr;
+      }
+    }
+    if (killed) {
+      visit_push(visits, cell, vis_a, vis_b);
+      active = 0;
+    } else if (collided) {
+      uniform_angle(&r, p->dir);
+      if (rng_next(&r) > (sigma_s / ((1.0 - f) * sigma_a + sigma_s)))
+        p->group = sample_emission_group(&r, sigma_a, m->n_groups);
+    } else if (dist_to_event == dist_to_boundary) {
+      int interior;
+      switch (surface_cross) {
+      case 0: interior = ci > 0; break;
+      case 1: interior = ci + 1 < m->ngx; break;
+      case 2: interior = cj > 0; break;
+      case 3: interior = cj + 1 < m->ngy; break;
+      case 4: interior = ck > 0; break;
+      default: interior = ck + 1 < m->ngz; break;
+      }
+      const int bc = interior ? BO_ELEMENT : m->bc[surface_cross];
+      if (bc == BO_ELEMENT) {
+        visit_push(visits, cell, vis_a, vis_b);
+        vis_a = 0.0;
+        vis_b = 0.0;
+        switch (surface_cross) {
+        case 0: --ci; cell -= 1; break;
+        case 1: ++ci; cell += 1; break;
+        case 2: --cj; cell -= m->ngx; break;
+        case 3: ++cj; cell += m->ngx; break;
+        case 4: --ck; cell -= sxy; break;
+        default: ++ck; cell += sxy; break;
+        }
+        nodes[0] = m->x[ci]; nodes[1] = m->x[ci + 1];
+        nodes[2] = m->y[cj]; nodes[3] = m->y[cj + 1];
+        nodes[4] = m->z[ck]; nodes[5] = m->z[ck + 1];
+      } else if (bc == BO_VACUUM || bc == BO_SOURCE || bc == BO_PROCESSOR) {
+        visit_push(visits, cell, vis_a, vis_b);
+        active = 0;
+      } else {
+        p->dir[surface_cross / 2] = -p->dir[surface_cross / 2];
+      }
+    } else { /* census */
+      visit_push(visits, cell, vis_a, vis_b);
+      active = 0;
+    }
+  }
+  if (L_rw) *L_rw = acc_rw;
+  return prefix;
+}
+
+static bo_adj_coef *adjoint_coefs(const bo_cells *c, size_t n_cells) {
+  bo_adj_coef *k = (bo_adj_coef *)malloc(n_cells * sizeof(bo_adj_coef));
+  for (size_t g = 0; g < n_cells; ++g) {
+    const double op_a = c->op_a[g], op_s = c->op_s[g], f = c->f[g];
+    const double sig_eff = (1.0 - f) * op_a + op_s;
+    k[g].f2 = f * f;
+    k[g].g2 = 1.0 - f * f;
+    k[g].inv_se = sig_eff > 0.0 ? 1.0 / sig_eff : 0.0;
+    k[g].src = op_a > 0.0 ? f / op_a : 0.0;
+  }
+  return k;
+}
+
+uint64_t bo_adjoint_replay(const bo_mesh *m, const bo_cells *c, uint32_t seed, const bo_photon *start,
+                           size_t n, const double *w, int scale, double visit_bound, double *grad,
+                           int n_threads) {
+  const size_t n_cells = (size_t)m->ngx * m->ngy * m->ngz;
+  bo_adj_coef *k = adjoint_coefs(c, n_cells);
+  int nt = 1;
+#ifdef _OPENMP
+  nt = n_threads > 0 ? n_threads : omp_get_max_threads();
+#else
+  (void)n_threads;
+#endif
+  unsigned __int128 *sums = (unsigned __int128 *)calloc((size_t)nt * n_cells, sizeof(unsigned __int128));
+  uint64_t range_errors = 0;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nt) reduction(+ : range_errors)
+#endif
+  {
+    int t = 0;
+#ifdef _OPENMP
+    t = omp_get_thread_num();
+#endif
+    unsigned __int128 *mine = sums + (size_t)t * n_cells;
+    bo_visit_log log = {NULL, 0, 0};
+#ifdef _OPENMP
+#pragma omp for schedule(guided)
+#endif
+    for (long i = 0; i < (long)n; ++i) {
+      const double G = adjoint_replay_photon(m, c, k, seed, &start[i], w, &log, NULL, NULL, NULL);
+      for (size_t v = 0; v < log.n; ++v) {
+        const double val = G * log.v[v].a - log.v[v].b;
+        if (val == 0.0) continue;
+        if (!(fabs(val) <= visit_bound)) {
+          ++range_errors;
+          continue;
+        }
+        mine[log.v[v].cell] += fixed128_signed(val, scale);
+      }
+    }
+    free(log.v);
+  }
+  for (size_t g = 0; g < n_cells; ++g) {
+    unsigned __int128 acc = 0;
+    for (int t = 0; t < nt; ++t) acc += sums[(size_t)t * n_cells + g];
+    grad[g] = fixed128_to_double(acc, scale);
+  }
+  free(sums);
+  free(k);
+  return range_errors;
+}
+
+double bo_adjoint_reweighted(const bo_mesh *m, const bo_cells *c, const double *op_a_p, const double *f_p,
+                             uint32_t seed, const bo_photon *start, size_t n, const double *w) {
+  const size_t n_cells = (size_t)m->ngx * m->ngy * m->ngz;
+  bo_adj_coef *k = adjoint_coefs(c, n_cells);
+  bo_visit_log log = {NULL, 0, 0};
+  double L = 0.0;
+  for (size_t i = 0; i < n; ++i) {
+    double l = 0.0;
+    adjoint_replay_photon(m, c, k, seed, &start[i], w, &log, op_a_p, f_p, &l);
+    L += l;
+  }
+  free(log.v);
+  free(k);
+  return L;
+}

@@ -106,6 +106,20 @@ size_t bo_post_process(double next_dt, bo_photon *photons, size_t n, bo_photon *
 void bo_update_temperature(const bo_mesh *m, bo_cells *c, double dt, double *abs_E,
                            double *track_E, double *total_abs_E, double *post_mat_E);
 
+/* Adjoint replay (no upstream counterpart): dL/dsigma_a per cell for
+ * L = sum_c w_c abs_E[c], from the start states of one step's photons and
+ * the step's op_a/op_s/f, with the estimator and the 128-bit fixed-point
+ * sums (exponent `scale`) of the GPU backward.  Visits whose contribution
+ * exceeds visit_bound are dropped and counted (the return value). */
+uint64_t bo_adjoint_replay(const bo_mesh *m, const bo_cells *c, uint32_t seed, const bo_photon *start,
+                           size_t n, const double *w, int scale, double visit_bound, double *grad,
+                           int n_threads);
+/* L at perturbed opacities/Fleck factors (op_a_p, f_p) estimated on the
+ * unperturbed paths with causal likelihood ratios; its finite difference
+ * reproduces bo_adjoint_replay's per-history terms. */
+double bo_adjoint_reweighted(const bo_mesh *m, const bo_cells *c, const double *op_a_p, const double *f_p,
+                             uint32_t seed, const bo_photon *start, size_t n, const double *w);
+
 #ifdef __cplusplus
 }
 #endif

@@ -97,6 +97,12 @@ def lib():
         L.bo_post_process.argtypes = [C.c_double, pp, C.c_size_t, pp, dp, dp]
         L.bo_update_temperature.argtypes = [C.POINTER(_Mesh), C.POINTER(_Cells), C.c_double, dp, dp,
                                             dp, dp]
+        L.bo_adjoint_replay.restype = C.c_uint64
+        L.bo_adjoint_replay.argtypes = [C.POINTER(_Mesh), C.POINTER(_Cells), C.c_uint32, pp, C.c_size_t, dp,
+                                        C.c_int, C.c_double, dp, C.c_int]
+        L.bo_adjoint_reweighted.restype = C.c_double
+        L.bo_adjoint_reweighted.argtypes = [C.POINTER(_Mesh), C.POINTER(_Cells), dp, dp, C.c_uint32, pp,
+                                            C.c_size_t, dp]
         _lib = L
     return _lib
 
@@ -224,6 +230,40 @@ class Oracle:
         elapsed = time.perf_counter() - t0
         return abs_E, track_E, census[:nc].copy(), ce.value, ex.value, int(segs), elapsed
 
+    def adjoint(self, start: np.ndarray, w: np.ndarray, scale: int, visit_bound: float,
+                n_threads: Optional[int] = None):
+        """dL/dsigma_a of L = sum w*abs_E by the CPU replay of the adjoint
+        estimator over the step's start photons, at the op_a/op_s/f of the
+        step's energies (still in the cell arrays after the step); returns
+        (gradient, visits dropped as out of range)."""
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        grad = np.zeros(self.n_cells)
+        start = np.ascontiguousarray(start)
+        bad = lib().bo_adjoint_replay(C.byref(self.mesh), C.byref(self.cells), self.deck.seed, start.ctypes.data,
+                                      len(start), _dptr(w), int(scale), float(visit_bound), _dptr(grad),
+                                      self.n_threads if n_threads is None else n_threads)
+        return grad, int(bad)
+
+    def reweighted_L(self, start: np.ndarray, w: np.ndarray, op_a_p: np.ndarray, f_p: np.ndarray) -> float:
+        """L at perturbed opacities estimated on the unperturbed paths with
+        likelihood ratios (its finite difference is the adjoint estimator)."""
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        op_a_p = np.ascontiguousarray(op_a_p, dtype=np.float64)
+        f_p = np.ascontiguousarray(f_p, dtype=np.float64)
+        start = np.ascontiguousarray(start)
+        return float(lib().bo_adjoint_reweighted(C.byref(self.mesh), C.byref(self.cells), _dptr(op_a_p),
+                                                 _dptr(f_p), self.deck.seed, start.ctypes.data, len(start),
+                                                 _dptr(w)))
+
+    def fleck(self, op_a: np.ndarray, dt: float) -> np.ndarray:
+        """Fleck factor per cell for the given opacities at the current
+        temperatures (mesh.h:267)."""
+        regs = self.deck.region_table()
+        reg = self.deck.cell_regions()
+        cv, rho = regs[reg, 0], regs[reg, 1]
+        T = self.arr["T_e"]
+        return 1.0 / (1.0 + dt * op_a * C_LIGHT * (4.0 * 0.01372 * T ** 3.0 / (cv * rho)))
+
     def step(self) -> StepResult:
         L = lib()
         step = self.step_no
@@ -250,6 +290,25 @@ class Oracle:
         self.dt = nd
         self.step_no += 1
         return res
+
+
+def adjoint_scale(w, start, op_a, op_s, f, n_segments):
+    """Fixed-point exponent and per-visit bound of the gradient sums, by the
+    rule the GPU backward applies (bgs_adjoint_api.cu)."""
+    import math
+    w = np.asarray(w, np.float64)
+    wmax = float(np.max(np.abs(w))) if w.size else 0.0
+    max_E = float(np.max(np.abs(start["E"]))) if len(start) else 0.0
+    max_L = float(np.max(np.abs(start["life_dx"]))) if len(start) else 0.0
+    sig_eff = (1.0 - f) * op_a + op_s
+    inv_se = np.where(sig_eff > 0.0, 1.0 / np.where(sig_eff > 0.0, sig_eff, 1.0), 0.0)
+    src = np.where(op_a > 0.0, f / np.where(op_a > 0.0, op_a, 1.0), 0.0)
+    coef = float(max(np.max(np.abs(src)), np.max(np.abs((1.0 - f * f) * inv_se))))
+    bound = wmax * max_E * (3.0 * max_L + 8.0 * coef) * 4096.0
+    if not bound > 0.0:
+        return 0, bound
+    _, e = math.frexp(bound * float(n_segments + len(start) + 1))
+    return 118 - e, bound
 
 
 def read_harness_step(out_dir: str, step: int, n_cells: int) -> dict:

@@ -1,0 +1,143 @@
+"""Adjoint pair on the GPU through the C ABI (bgs_adjoint_forward/backward).
+
+  * parity: the GPU backward against the oracle's CPU replay of the same
+    estimator over the same histories, cell by cell, with the fixed-point
+    exponent the GPU chose (the CPU forward is the parity-checked oracle);
+  * the forward with explicit opacities equal to the region law reproduces
+    the plain forward bit for bit, and backward is deterministic and linear
+    in dL/dE_abs;
+  * unbiasedness: against common-random-number central differences
+    (h = 1e-4 relative, photon counts frozen) on a problem whose gradient
+    is resolved, averaged over independent seeds;
+  * the torch.autograd wrapper returns the backward's gradient.
+"""
+import numpy as np
+import pytest
+
+from parity import CELL_RTOL, close
+
+pytestmark = pytest.mark.gpu
+
+
+def _decks():
+    from branson_gb300 import deck as D
+    return {
+        "random_cube8": D.random_opacity_cube(n_per_axis=8, photons=20000, seed=3),
+        "hot_zone10": D.hot_zone(n_per_axis=10, photons=20000, n_steps=1),
+        "marshak": D.marshak_wave(n_cells=100, photons=20000, n_steps=1),
+        "hohlraum10_g30": D.hohlraum(n_per_axis=10, photons=20000, n_steps=1, n_groups=30),
+    }
+
+
+@pytest.mark.parametrize("name", ["random_cube8", "hot_zone10", "marshak", "hohlraum10_g30"])
+def test_backward_matches_cpu_replay(gpu_lib, name):
+    import oracle as O
+    from branson_gb300.adjoint import AdjointStep
+
+    dk = _decks()[name]
+    orc = O.Oracle(dk, n_threads=8)
+    _, photons = orc.source(1)
+    start = photons.copy()
+    abs_o, _, _, _, _, segs, _ = orc.transport(photons, orc.next_dt())
+    with AdjointStep(dk) as st:
+        abs_g, tape = st.forward()
+        close(abs_g, abs_o, CELL_RTOL, 0.0, f"{name} forward abs_E")
+        w = np.random.default_rng(7).uniform(-1.0, 1.0, st.n_cells)
+        g = st.backward(tape, w)
+        info = tape.info()
+        assert info["n_histories"] == len(start) and info["n_segments"] == segs
+        assert info["device_flags"] == 0
+        go, dropped = orc.adjoint(start, w, info["grad_scale"], info["visit_bound"])
+        assert dropped == 0
+        close(g, go, CELL_RTOL, 0.0, f"{name} dL/dsigma_a")
+        tape.close()
+
+
+def test_forward_override_repeat_and_linearity(gpu_lib):
+    from branson_gb300 import deck as D
+    from branson_gb300.adjoint import AdjointStep
+
+    dk = D.random_opacity_cube(n_per_axis=6, photons=30000, seed=5)
+    sig = np.array([r.opacA for r in dk.regions])[dk.cell_regions()]
+    with AdjointStep(dk) as st:
+        a0, t0 = st.forward()
+        a1, t1 = st.forward(sigma_a=sig)
+        np.testing.assert_array_equal(a0, a1)
+        counts = t1.counts()
+        a2, _ = st.forward(sigma_a=sig, counts=counts, save=False)
+        np.testing.assert_array_equal(a0, a2)
+        rng = np.random.default_rng(1)
+        w1, w2 = rng.uniform(0, 1, st.n_cells), rng.uniform(-1, 1, st.n_cells)
+        g0 = st.backward(t0, w1)
+        np.testing.assert_array_equal(g0, st.backward(t1, w1))
+        np.testing.assert_array_equal(g0, st.backward(t0, w1))
+        g2 = st.backward(t0, w2)
+        g12 = st.backward(t0, w1 + w2)
+        np.testing.assert_allclose(g12, g0 + g2, rtol=1e-9, atol=1e-12 * np.max(np.abs(g12)))
+        t0.close()
+        t1.close()
+
+
+def _row_deck(sig, photons, seed):
+    from branson_gb300.deck import Deck, Division, Region, VACUUM
+    n = len(sig)
+    return Deck(t_start=0.0, t_stop=0.01, dt_start=0.01, t_mult=1.0, dt_max=1.0, photons=photons, seed=seed,
+                x_divisions=[Division(i / n, (i + 1) / n, 1) for i in range(n)],
+                y_divisions=[Division(0.0, 1.0 / n, 1)], z_divisions=[Division(0.0, 1.0 / n, 1)],
+                region_map={(i, 0, 0): i + 1 for i in range(n)}, bc=(VACUUM,) * 6, T_source=0.0,
+                regions=[Region(i + 1, 0.1, 1.0, float(s), 0.0, 0.0, 0.0, 0.1, 0.1) for i, s in enumerate(sig)])
+
+
+def test_gradient_agrees_with_crn_finite_differences(gpu_lib):
+    """Four optically thick cells (sigma_a 20/cm, 0.25 cm), emission only:
+    every cell's gradient is resolved.  Per seed, the adjoint and the CRN
+    central difference (h = 1e-4 relative, counts frozen) use the same
+    photons; over 8 seeds the means must agree within 2% (the estimator does
+    not differentiate the E/E0 < 0.01 cutoff, worth a few tenths of a
+    percent here) plus three standard errors of the paired difference."""
+    from branson_gb300.adjoint import AdjointStep
+
+    sig = np.array([20.0, 12.0, 30.0, 20.0])
+    w = np.array([0.3, 0.9, 0.1, 0.7])
+    h = 1e-4
+    adj, fd = [], []
+    for seed in range(1, 9):
+        with AdjointStep(_row_deck(sig, 200000, seed)) as st:
+            _, tape = st.forward(sigma_a=sig)
+            counts = tape.counts()
+            adj.append(st.backward(tape, w))
+            row = []
+            for j in range(len(sig)):
+                sp, sm = sig.copy(), sig.copy()
+                sp[j] *= 1 + h
+                sm[j] *= 1 - h
+                ap, _ = st.forward(sigma_a=sp, counts=counts, save=False)
+                am, _ = st.forward(sigma_a=sm, counts=counts, save=False)
+                row.append(np.dot(w, ap - am) / (2 * h * sig[j]))
+            fd.append(row)
+            tape.close()
+    adj, fd = np.array(adj), np.array(fd)
+    d = adj - fd
+    se = d.std(axis=0, ddof=1) / np.sqrt(len(d))
+    for j in range(len(sig)):
+        print(f"cell {j}: adjoint {adj[:, j].mean():.6e} fd {fd[:, j].mean():.6e} "
+              f"rel {d[:, j].mean() / abs(fd[:, j].mean()):+.4f} (se {se[j] / abs(fd[:, j].mean()):.4f})")
+        assert abs(d[:, j].mean()) <= 0.02 * abs(fd[:, j].mean()) + 3.0 * se[j], j
+
+
+def test_autograd_function(gpu_lib):
+    import torch
+    from branson_gb300 import deck as D
+    from branson_gb300.adjoint import AdjointStep, absorbed_energy
+
+    dk = D.random_opacity_cube(n_per_axis=4, photons=20000, seed=9)
+    sig0 = np.array([r.opacA for r in dk.regions])[dk.cell_regions()]
+    w = np.random.default_rng(3).uniform(0, 1, len(sig0))
+    with AdjointStep(dk) as st:
+        sig = torch.tensor(sig0, dtype=torch.float64, requires_grad=True)
+        E = absorbed_energy(st, sig)
+        L = (torch.from_numpy(w) * E).sum()
+        L.backward()
+        _, tape = st.forward(sigma_a=sig0)
+        np.testing.assert_array_equal(sig.grad.numpy(), st.backward(tape, w))
+        tape.close()
