@@ -59,6 +59,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--cpu-photons", type=float, default=1e6)
     p.add_argument("--no-adjoint", action="store_true")
+    p.add_argument("--no-batch", action="store_true")
+    p.add_argument("--batch-problems", type=int, default=256)
     p.add_argument("--adjoint-photons", type=float, default=1e7)
     return p.parse_args()
 
@@ -301,6 +303,9 @@ def run_ours(args, rank, world, local):
     adjoint = None
     if not args.no_adjoint and rank == 0 and world == 1:
         adjoint = adjoint_bench(args, dev)
+    batched = None
+    if not args.no_batch and rank == 0 and world == 1:
+        batched = batch_bench(args, dev)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
@@ -308,7 +313,7 @@ def run_ours(args, rank, world, local):
                 "config": dict(cfg, parallelism=f"replicas{world}"), "roofline": roofline,
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
                 "segments_per_s": segs / elapsed * world, "histories_per_step": hist / args.steps,
-                "adjoint": adjoint}
+                "adjoint": adjoint, "batched": batched}
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -344,6 +349,68 @@ def e2e_dropin(imc, dk, args):
         + 2 * 8 * dk.n_cells
     return {"value": hist / secs, "unit": UNIT, "h2d_bytes_per_step": int(in_bytes),
             "d2h_bytes_per_step": int(out_bytes), "call": "bgs_replicated_transport", "steps": k}
+
+
+def batch_bench(args, dev, steps: int = 2):
+    """Batching workload: 256 independent problems (master seed 777), cubic
+    meshes of side U{8..64} on [0,1]^3, photons lognormal (median 1e5)
+    clipped to [1e4, 1e6], per-problem sigma_a ~ U(1,200) and source T ~
+    U(0.2,1) on x-, T0 = 0.01 keV, steps of 0.005 sh.  Sequential: every
+    problem on its own context, one bgs_step after another, each waited for
+    (the plain launches).  Batched: the same problems on fresh contexts
+    through bgs_batch_step (one persistent transport launch, the step
+    recorded as one CUDA graph and launched with one call).  Each arm starts
+    from step 1 and times `steps` steps (wall clock around each whole step);
+    histories/s = histories of all problems / that time."""
+    from branson_gb300 import deck as D
+    from branson_gb300.engine import BatchIMC, ReplicatedIMC
+
+    n = args.batch_problems
+    decks = D.batch_ensemble(n_problems=n, master_seed=777)
+    # warm-up of the batched path (module load, graph machinery) on a small ensemble
+    with BatchIMC(D.batch_ensemble(n_problems=4, master_seed=1, side_range=(4, 8), photon_median=2000,
+                                   photon_range=(1000, 4000)), device=dev) as w:
+        w.step(sync=True)
+    seq = {"s": [], "hist": [], "seg": [], "transport_ms": []}
+    probs = [ReplicatedIMC(dk, device=dev) for dk in decks]
+    try:
+        for _ in range(steps):
+            reps, kms = [], 0.0
+            t0 = time.perf_counter()
+            for p in probs:
+                reps.append(p.step(sync=True))
+                kms += p.last_transport_ms()[0]
+            seq["s"].append(time.perf_counter() - t0)
+            seq["hist"].append(sum(r.n_transported for r in reps))
+            seq["seg"].append(sum(r.n_segments for r in reps))
+            seq["transport_ms"].append(kms)
+    finally:
+        for p in probs:
+            p.close()
+    bat = {"s": [], "hist": [], "seg": [], "transport_ms": []}
+    with BatchIMC(decks, device=dev) as b:
+        launches0 = b.last_transport_ms()[1]
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            reps = b.step(sync=True)
+            bat["s"].append(time.perf_counter() - t0)
+            bat["hist"].append(sum(r.n_transported for r in reps))
+            bat["seg"].append(sum(r.n_segments for r in reps))
+            bat["transport_ms"].append(b.last_transport_ms()[0])
+        launches = b.last_transport_ms()[1] - launches0
+    assert seq["hist"] == bat["hist"] and seq["seg"] == bat["seg"], "batched and sequential runs disagree"
+    rate_s = sum(seq["hist"]) / sum(seq["s"])
+    rate_b = sum(bat["hist"]) / sum(bat["s"])
+    return {"workload": f"batch_ensemble of {n} problems (side U{{8..64}}, photons lognormal median 1e5 in "
+                        "[1e4, 1e6], sigma_a U(1,200), T_source U(0.2,1)), steps from step 1",
+            "steps": steps, "histories_per_step": seq["hist"], "segments_per_step": seq["seg"],
+            "sequential_hist_per_s": rate_s, "batched_hist_per_s": rate_b, "batched_over_sequential": rate_b / rate_s,
+            "sequential_step_s": seq["s"], "batched_step_s": bat["s"],
+            "batched_transport_kernel_ms": bat["transport_ms"],
+            "sequential_transport_kernel_ms_sum": seq["transport_ms"],
+            "batched_segments_per_s": sum(bat["seg"]) / sum(bat["s"]),
+            "kernel_launches_per_batched_step": launches // steps,
+            "timing": "host wall clock around each whole step (sync), same problems and results in both arms"}
 
 
 def adjoint_bench(args, dev, replicas: int = 6):

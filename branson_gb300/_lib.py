@@ -21,6 +21,7 @@ REFLECT, VACUUM, ELEMENT, SOURCE, PROCESSOR = range(5)
 EXIT, PASS, CENSUS, SCATTER, KILLED, BOUND = range(6)
 HISTORY, EVENT = 0, 1
 OPTIONS = {"event_round_cap": 0, "event_check_every": 1, "event_tail_fraction": 2, "transport_blocks": 3}
+BATCH_OPTIONS = {"graph": 0, "transport_blocks": 1}
 FIELDS = {"T_e": 0, "T_r": 1, "op_a": 2, "op_s": 3, "f": 4, "emission_E": 5, "census_E": 6,
           "source_E": 7, "abs_E": 8, "track_E": 9}
 
@@ -107,6 +108,13 @@ SIGNATURES = (
     ("bgs_adjoint_counts", C.c_int, [C.c_void_p, C.c_void_p]),
     ("bgs_adjoint_get_info", C.c_int, [C.c_void_p, C.POINTER(AdjointInfo)]),
     ("bgs_adjoint_release", C.c_int, [C.c_void_p]),
+    ("bgs_batch_create", C.c_int, [C.POINTER(C.c_void_p), C.c_uint32, C.POINTER(C.c_void_p)]),
+    ("bgs_batch_destroy", C.c_int, [C.c_void_p]),
+    ("bgs_batch_last_error", C.c_char_p, [C.c_void_p]),
+    ("bgs_batch_step", C.c_int, [C.c_void_p, C.POINTER(StepParams), C.POINTER(TransportDiag)]),
+    ("bgs_batch_synchronize", C.c_int, [C.c_void_p]),
+    ("bgs_batch_set_option", C.c_int, [C.c_void_p, C.c_int, C.c_double]),
+    ("bgs_batch_last_transport_ms", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_uint64)]),
     ("bgs_set_option", C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     ("bgs_last_transport_ms", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_uint32)]),
     ("bgs_kernel_launch_count", C.c_uint64, [C.c_void_p]),

@@ -409,9 +409,7 @@ int transport_event(bgs_context *ctx, const Bank &from) {
 
 }  // namespace
 
-int run_transport(bgs_context *ctx, const Bank &from, uint32_t algorithm) {
-  if (algorithm != BGS_HISTORY && algorithm != BGS_EVENT)
-    return fail(ctx, BGS_ERR_INVALID, "unknown transport algorithm %u", algorithm);
+int prepare_transport(bgs_context *ctx, const Bank &from) {
   if (ctx->xs_dirty) {
     launch_cell_xs(ctx->mesh, ctx->cells, ctx->stream);
     BGS_LAUNCHED(ctx, 1);
@@ -422,9 +420,16 @@ int run_transport(bgs_context *ctx, const Bank &from, uint32_t algorithm) {
   BGS_CUDA(ctx, cudaMemsetAsync(ctx->cells.tally, 0, ctx->mesh.n_cells * sizeof(TallyCell), ctx->stream));
   k_reset_queue<<<1, 1, 0, ctx->stream>>>(ctx->d_diag);
   BGS_LAUNCHED(ctx, 1);
+  return BGS_OK;
+}
+
+int run_transport(bgs_context *ctx, const Bank &from, uint32_t algorithm) {
+  if (algorithm != BGS_HISTORY && algorithm != BGS_EVENT)
+    return fail(ctx, BGS_ERR_INVALID, "unknown transport algorithm %u", algorithm);
+  int rc;
+  if ((rc = prepare_transport(ctx, from))) return rc;
   BGS_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
   if (algorithm == BGS_EVENT) {
-    int rc;
     if ((rc = transport_event(ctx, from))) return rc;
   } else {
     launch_transport_history(ctx->mesh, ctx->cells, from, ctx->d_diag, ctx->seed, ctx->tshape, ctx->stream);
@@ -434,14 +439,9 @@ int run_transport(bgs_context *ctx, const Bank &from, uint32_t algorithm) {
   return BGS_OK;
 }
 
-namespace {
-
-int transport_impl(bgs_context *ctx, double next_dt, uint32_t algorithm) {
-  const uint64_t before = ctx->launches;
+int finish_transport(bgs_context *ctx, double next_dt) {
   Bank &from = ctx->bank[ctx->cur];
   Bank &to = ctx->bank[1 - ctx->cur];
-  int rc;
-  if ((rc = run_transport(ctx, from, algorithm))) return rc;
   launch_scan_flags(from.desc, CENSUS, (uint32_t)ctx->capacity, &ctx->d_diag->n_bank, ctx->d_off_bank,
                     ctx->d_tile_bank, ctx->stream);
   BGS_LAUNCHED(ctx, 3);
@@ -449,9 +449,19 @@ int transport_impl(bgs_context *ctx, double next_dt, uint32_t algorithm) {
   BGS_LAUNCHED(ctx, 2);
   launch_tally_to_double(ctx->mesh, ctx->cells, ctx->d_diag, ctx->d_abs, ctx->d_track, ctx->stream);
   BGS_LAUNCHED(ctx, 2);
-  ctx->last_launches = (uint32_t)(ctx->launches - before);
   ctx->cur = 1 - ctx->cur;
   ctx->bank_is_census = true;
+  return BGS_OK;
+}
+
+namespace {
+
+int transport_impl(bgs_context *ctx, double next_dt, uint32_t algorithm) {
+  const uint64_t before = ctx->launches;
+  int rc;
+  if ((rc = run_transport(ctx, ctx->bank[ctx->cur], algorithm))) return rc;
+  if ((rc = finish_transport(ctx, next_dt))) return rc;
+  ctx->last_launches = (uint32_t)(ctx->launches - before);
   return BGS_OK;
 }
 

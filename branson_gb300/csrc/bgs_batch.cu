@@ -1,0 +1,205 @@
+// One persistent transport launch over many independent problems.
+//
+// Each problem keeps its own context (mesh, cell table, tallies, banks,
+// device scalars); a device table of ProblemView descriptors points at
+// them (the other phases of a batched step run as launches over the same
+// table, one problem per blockIdx.y: bgs_mesh.cu, bgs_source.cu,
+// bgs_transport.cu).  Work items are the concatenation of every problem's bank
+// (exclusive prefix sum of the problems' n_bank, formed on the device, so
+// no count goes through the host); each warp pulls items from one global
+// queue, a lane finds its problem by binary search at pickup and then runs
+// the history exactly as k_transport_history does (same per-segment code
+// from bgs_physics.cuh, the problem's seed, tallies and fixed-point scales),
+// so every problem's end states and tallies are those of its own launch.
+// Small problems no longer leave the GPU idle: the tail of one overlaps the
+// bulk of the others.
+#include "bgs_physics.cuh"
+
+namespace bgs {
+
+constexpr int kItemThreads = 1024;
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// work_counter[0]: queue head; [1], [2]: first block start and last block
+// end of the batched launch (global timer, ns), so the launch can be timed
+// inside a CUDA graph
+__global__ void __launch_bounds__(kItemThreads) k_batch_items(const ProblemView *probs, uint32_t n,
+                                                              unsigned long long *item_off,
+                                                              unsigned long long *work_counter) {
+  __shared__ unsigned long long s_warp[kItemThreads / 32];
+  __shared__ unsigned long long s_carry;
+  if (threadIdx.x == 0) s_carry = 0;
+  __syncthreads();
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  for (uint32_t base = 0; base < n; base += kItemThreads) {
+    const uint32_t p = base + threadIdx.x;
+    const unsigned long long v = p < n ? probs[p].d->n_bank : 0ULL;
+    unsigned long long incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= (unsigned)o) incl += t;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+      unsigned long long w = s_warp[lane];
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long t = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= (unsigned)o) w += t;
+      }
+      s_warp[lane] = w;  // inclusive over warps
+    }
+    __syncthreads();
+    const unsigned long long before = s_carry + (warp > 0 ? s_warp[warp - 1] : 0ULL) + incl - v;
+    if (p < n) item_off[p] = before;
+    __syncthreads();
+    if (threadIdx.x == kItemThreads - 1) s_carry = before + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    item_off[n] = s_carry;
+    work_counter[0] = 0;
+    work_counter[1] = ~0ULL;
+    work_counter[2] = 0;
+  }
+}
+
+// problem of item w: the last p with item_off[p] <= w
+__device__ __forceinline__ uint32_t problem_of(const unsigned long long *item_off, uint32_t n,
+                                               unsigned long long w) {
+  uint32_t lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (item_off[mid] <= w) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ void flush_batched(const ProblemView &P, uint32_t cell, double a, double t,
+                                              uint32_t &flags) {
+  const DeviceDiag *d = P.d;
+  flush_tally(P.c, d, cell, a, t, flags, d->scale_abs, d->scale_track);
+}
+
+__global__ void __launch_bounds__(kTransportThreads, BGS_MIN_BLOCKS)
+    k_transport_batched(const ProblemView *__restrict__ probs, uint32_t n_probs,
+                        const unsigned long long *__restrict__ item_off, unsigned long long *work_counter) {
+  const unsigned long long n = item_off[n_probs];
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned lanemask_lt = (1u << lane) - 1u;
+  if (threadIdx.x == 0) atomicMin(&work_counter[1], global_ns());
+  uint32_t flags = 0;
+  Lane L;
+  uint32_t p = 0;
+  const CellXS *xs_p = nullptr;
+  bool active = false, done = false;
+
+  while (true) {
+    const unsigned need = __ballot_sync(0xffffffffu, !active && !done);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      unsigned long long base = 0;
+      if ((int)lane == leader) base = atomicAdd(work_counter, (unsigned long long)__popc(need));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (!active && !done) {
+        const unsigned long long w = base + __popc(need & lanemask_lt);
+        if (w < n) {
+          p = problem_of(item_off, n_probs, w);
+          const ProblemView &P = probs[p];
+          const unsigned long long i = w - item_off[p];
+          const Bank &b = P.from;
+          L.idx = i;
+          L.px = b.px[i]; L.py = b.py[i]; L.pz = b.pz[i];
+          L.dx = b.dx[i]; L.dy = b.dy[i]; L.dz = b.dz[i];
+          L.E = b.E[i]; L.E0 = b.E0[i]; L.life = b.life[i];
+          L.cell = b.cell[i]; L.group = b.group[i];
+          L.rng.stream = b.stream[i]; L.rng.ctr = b.ctr[i]; L.rng.hi = P.seed_hi;
+          L.segs = 0;
+          L.thr_abs = 0.0; L.thr_trk = 0.0;
+          L.inv_E0 = 1.0 / L.E0;
+          direction_recips(L);
+          xs_p = P.c.xs;
+          if (L.cell < P.m.n_cells) {
+            locate(P.m, L);
+            active = true;
+          } else {
+            atomicOr(&P.d->flags, (uint32_t)FLAG_BAD_CELL);
+            b.desc[i] = KILLED;
+          }
+        } else {
+          done = true;
+        }
+      }
+    }
+    if (__all_sync(0xffffffffu, !active)) break;
+    if (!active) continue;
+
+    // ---- one segment of transport_photon (history_based_transport.h:55-139)
+    const CellXS xs = xs_p[L.cell];
+    uint32_t surface_cross;
+    const int ev = segment_advance(xs, L, surface_cross, flags);
+    bool end = false;
+    uint8_t desc = KILLED;
+    if (ev == SEG_KILLED) {
+      end = true;
+    } else if (ev == SEG_SCATTER) {
+      scatter_update(probs[p].m, probs[p].c, xs, L);
+    } else if (ev == SEG_BOUNDARY) {
+      const MeshDev &m = probs[p].m;
+      const int bc = face_bc(m, L, surface_cross);
+      if (bc == ELEMENT) {
+        flush_batched(probs[p], L.cell, L.thr_abs, L.thr_trk, flags);
+        L.thr_abs = 0.0;
+        L.thr_trk = 0.0;
+        enter_neighbour(m, L, surface_cross);
+      } else if (bc == VACUUM || bc == SOURCE || bc == PROCESSOR) {
+        end = true;
+        desc = bc == PROCESSOR ? PASS : EXIT;
+      } else {
+        reflect(L, surface_cross);
+      }
+    } else {  // SEG_CENSUS
+      end = true;
+      desc = CENSUS;
+    }
+    if (end) {
+      const ProblemView &P = probs[p];
+      flush_batched(P, L.cell, L.thr_abs, L.thr_trk, flags);
+      store_end(P.from, L, desc);
+      atomicAdd(&P.d->n_segments, (unsigned long long)L.segs);
+      if (flags) {
+        atomicOr(&P.d->flags, flags);
+        flags = 0;
+      }
+      active = false;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) atomicMax(&work_counter[2], global_ns());
+}
+
+TransportLaunch batch_launch_shape(int n_sm) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_transport_batched, kTransportThreads, 0) !=
+          cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  return {n_sm * per_sm, kTransportThreads};
+}
+
+void launch_batch_items(const ProblemView *probs, uint32_t n, unsigned long long *item_off,
+                        unsigned long long *work_counter, cudaStream_t s) {
+  k_batch_items<<<1, kItemThreads, 0, s>>>(probs, n, item_off, work_counter);
+}
+
+void launch_transport_batched(const ProblemView *probs, uint32_t n, const unsigned long long *item_off,
+                              unsigned long long *work_counter, const TransportLaunch &shape, cudaStream_t s) {
+  k_transport_batched<<<shape.blocks, shape.threads, 0, s>>>(probs, n, item_off, work_counter);
+}
+
+}  // namespace bgs

@@ -135,6 +135,12 @@ inline int read_diag(bgs_context *ctx) {
   return BGS_OK;
 }
 
-// transport of every photon in `from` (history or event mode) into the
-// context's tallies; defined in bgs_api.cu
+// Transport phases (bgs_api.cu).  prepare_transport: per-cell table if
+// stale, fixed-point scales from the bank, zeroed tallies and work queue.
+// run_transport: prepare + every photon in `from` transported (history or
+// event mode) into the context's tallies.  finish_transport: census
+// compaction into the other bank (which becomes current) and the tallies
+// converted to doubles.
+int prepare_transport(bgs_context *ctx, const Bank &from);
 int run_transport(bgs_context *ctx, const Bank &from, uint32_t algorithm);
+int finish_transport(bgs_context *ctx, double next_dt);

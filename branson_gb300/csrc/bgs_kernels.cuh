@@ -22,6 +22,34 @@ __device__ __forceinline__ double cell_volume(const double n[6]) {
   return (n[1] - n[0]) * (n[3] - n[2]) * (n[5] - n[4]);
 }
 
+// x^n for a small integer n >= 0 (the temperature powers of
+// calculate_photon_energy), rounded once: the running product is kept as an
+// unevaluated double-double sum with exact products (Dekker's TwoProduct
+// via fma), so the result is the correctly rounded power except when the
+// exact value lies within ~n*2^-105 relative of a rounding boundary.  Zero,
+// non-finite and out-of-range arguments take pow.
+__device__ __forceinline__ double pow_small_int_rn(double x, int n) {
+  if (n == 0) return 1.0;
+  if (!(x > 0.0) || !isfinite(x) || x > 1e60 || x < 1e-60) return pow(x, (double)n);
+  double ph = x, pl = 0.0;
+  for (int i = 1; i < n; ++i) {
+    const double p = __dmul_rn(ph, x);
+    const double e = __fma_rn(ph, x, -p);   // ph*x - p, exact
+    const double l = __fma_rn(pl, x, e);
+    const double s = __dadd_rn(p, l);
+    pl = __dsub_rn(l, __dsub_rn(s, p));     // |p| >= |l|: exact error of s
+    ph = s;
+  }
+  return ph;
+}
+
+// pow(x, c) with the small-integer exponents of the decks done exactly
+__device__ __forceinline__ double pow_deck(double x, double c) {
+  const int n = (int)c;
+  if ((double)n == c && n >= 0 && n <= 8) return pow_small_int_rn(x, n);
+  return pow(x, c);
+}
+
 // per-cell transport coefficients (see CellXS) and the CDF step of
 // sample_emission_group's walk, op_a(g) * 1/(op_a(0)*N) with all groups
 // equal (sampling_functions.h:132-135, cell.h:260-266)
@@ -41,7 +69,7 @@ __device__ __forceinline__ void set_cell_xs(const CellsDev &c, uint32_t g, doubl
 
 // ---------------------------------------------------------------- launchers
 void launch_init_cells(const MeshDev &m, const CellsDev &c, cudaStream_t s);
-uint32_t energy_parts(uint32_t n_cells);
+__host__ __device__ uint32_t energy_parts(uint32_t n_cells);
 void launch_cell_energy(const MeshDev &m, const CellsDev &c, uint32_t step, double dt, double *mat_E,
                         double *part, DeviceDiag *d, unsigned long long n_user, cudaStream_t s,
                         const double *op_a_in = nullptr);
@@ -82,6 +110,44 @@ void launch_transport_resume(const MeshDev &m, const CellsDev &c, const Bank &b,
 void launch_event_init(const EventState &es, DeviceDiag *d, cudaStream_t s);
 void launch_event_round(const MeshDev &m, const CellsDev &c, const Bank &b, DeviceDiag *d, uint32_t seed,
                         const EventState &es, bool first, int n_sm, cudaStream_t s);
+
+// Many independent problems stepped together (bgs_batch.cu): one problem's
+// view for the batched launches, in device memory.  Every batched kernel
+// takes the view table and runs problem blockIdx.y; the step's parameters
+// live in the table, so one recorded launch sequence serves every step.
+struct ProblemView {
+  MeshDev m;
+  CellsDev c;
+  DeviceDiag *d;
+  Bank from, to;             // this step's bank and the bank the census goes to
+  double *mat_E, *energy_part, *abs, *track, *mat_part;
+  unsigned long long *tile_cells, *off_bank, *tile_bank, *maxbits;
+  unsigned long long n_user, seed_hi;
+  uint32_t capacity, step;
+  double dt, next_dt;
+};
+TransportLaunch batch_launch_shape(int n_sm);
+// per-problem block counts of the batched launches
+struct BatchGrid {
+  uint32_t n;              // problems (gridDim.y)
+  uint32_t cells;          // blocks per problem over cells
+  uint32_t photons;        // blocks per problem over bank entries
+  uint32_t cell_tiles;     // scan tiles over the largest mesh
+  uint32_t bank_tiles;     // scan tiles over the largest bank capacity
+};
+// phases of one batched step, in order (bgs_mesh.cu, bgs_source.cu, bgs_batch.cu, bgs_transport.cu)
+void launch_batch_begin(const ProblemView *v, const BatchGrid &g, cudaStream_t s);
+void launch_batch_energy(const ProblemView *v, const BatchGrid &g, cudaStream_t s);
+void launch_batch_source(const ProblemView *v, const BatchGrid &g, cudaStream_t s);
+void launch_batch_bounds(const ProblemView *v, const BatchGrid &g, cudaStream_t s);
+// item offsets: exclusive prefix sum of every problem's n_bank (n+1 entries)
+void launch_batch_items(const ProblemView *v, uint32_t n, unsigned long long *item_off,
+                        unsigned long long *work_counter, cudaStream_t s);
+void launch_transport_batched(const ProblemView *v, uint32_t n, const unsigned long long *item_off,
+                              unsigned long long *work_counter, const TransportLaunch &shape, cudaStream_t s);
+void launch_batch_census_scan(const ProblemView *v, const BatchGrid &g, cudaStream_t s);
+void launch_batch_census(const ProblemView *v, const BatchGrid &g, cudaStream_t s);
+void launch_batch_finish(const ProblemView *v, const BatchGrid &g, cudaStream_t s);
 
 // adjoint replay of a saved photon bank (bgs_adjoint.cu)
 TransportLaunch adjoint_launch_shape(int n_sm);

@@ -13,9 +13,8 @@ namespace bgs {
 // sums, capacity check, and the transport work queue reset.  The bank holds
 // [census carried in | photons made this step]; at step 1 the carried census
 // is the initial census (make_initial_census_photons, source.h:183-204).
-__global__ void k_plan_bank(MeshDev m, CellsDev c, DeviceDiag *d, uint32_t step,
-                            unsigned long long capacity) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__device__ __forceinline__ void plan_bank_body(const MeshDev &m, const CellsDev &c, DeviceDiag *d, uint32_t step,
+                                               unsigned long long capacity) {
   const unsigned long long n_new = c.off_new[m.n_cells];
   const unsigned long long n_ic = step == 1 ? c.off_ce[m.n_cells] : 0ULL;
   if (step == 1) {
@@ -33,6 +32,12 @@ __global__ void k_plan_bank(MeshDev m, CellsDev c, DeviceDiag *d, uint32_t step,
   d->n_bank = d->n_census_in + made;
   d->work_counter = 0;
   d->n_segments = 0;
+}
+
+__global__ void k_plan_bank(MeshDev m, CellsDev c, DeviceDiag *d, uint32_t step,
+                            unsigned long long capacity) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  plan_bank_body(m, c, d, step, capacity);
 }
 
 // get_uniform_position_in_cell (sampling_functions.h:22-29)
@@ -74,12 +79,15 @@ __device__ __forceinline__ void position_on_face(const double n[6], Rng &r, int 
 // get_source_angle_on_face (sampling_functions.h:94-121): the inward sign is
 // applied on the x faces only, as upstream.
 __device__ __forceinline__ void source_angle(Rng &r, int face, double d[3]) {
-  const double theta = acos(sqrt(r.next()));
+  // theta = acos(sqrt(u)): cos(theta) = sqrt(u) and sin(theta) = sqrt(1-u)
+  // exactly, so both come from square roots instead of acos, sin and cos
+  const double u = r.next();
+  const double ct = sqrt(u);
+  const double st = sqrt(1.0 - u);
   const double phi = r.next() * 2.0 * kPi;
   const double sign = (face % 2) ? -1.0 : 1.0;
-  double st, ct, sp, cp;
-  sincos(theta, &st, &ct);
-  sincos(phi, &sp, &cp);
+  double sp, cp;
+  fix::sincos_phi(phi, &sp, &cp);
   if (face == 0 || face == 1) {
     d[0] = ct * sign;
     d[1] = st * sp;
@@ -120,11 +128,12 @@ __device__ __forceinline__ void store_photon(const Bank &b, unsigned long long i
 
 // Initial census photons (get_initial_census_photon, source.h:117-131):
 // stream = ith census photon (rank 0), 6 draws, life = c*dt.
-__global__ void k_source_census(MeshDev m, CellsDev c, Bank b, const DeviceDiag *d,
-                                unsigned long long seed_hi, double dt) {
+__device__ __forceinline__ void source_census_body(const MeshDev &m, const CellsDev &c, const Bank &b,
+                                                   const DeviceDiag *d, unsigned long long seed_hi, double dt,
+                                                   uint32_t bx, uint32_t nbx) {
   const unsigned long long n = d->n_init_census;
-  for (unsigned long long p = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; p < n;
-       p += (unsigned long long)gridDim.x * blockDim.x) {
+  for (unsigned long long p = bx * (unsigned long long)blockDim.x + threadIdx.x; p < n;
+       p += (unsigned long long)nbx * blockDim.x) {
     const uint32_t g = find_cell(c.off_ce, m.n_cells, p);
     double nodes[6], pos[3], dir[3];
     cell_nodes(m, g, nodes);
@@ -137,14 +146,20 @@ __global__ void k_source_census(MeshDev m, CellsDev c, Bank b, const DeviceDiag 
   }
 }
 
+__global__ void k_source_census(MeshDev m, CellsDev c, Bank b, const DeviceDiag *d,
+                                unsigned long long seed_hi, double dt) {
+  source_census_body(m, c, b, d, seed_hi, dt, blockIdx.x, gridDim.x);
+}
+
 // Emission (source.h:84-97, 7 draws) and boundary-source (source.h:100-114,
 // 6 draws) photons, stream = 1e13*cycle + ith photon, stored after the census.
-__global__ void k_source_new(MeshDev m, CellsDev c, Bank b, const DeviceDiag *d,
-                             unsigned long long seed_hi, uint32_t cycle, double dt) {
+__device__ __forceinline__ void source_new_body(const MeshDev &m, const CellsDev &c, const Bank &b,
+                                                const DeviceDiag *d, unsigned long long seed_hi, uint32_t cycle,
+                                                double dt, uint32_t bx, uint32_t nbx) {
   const unsigned long long n = d->n_new, base = d->n_census_in;
   const unsigned long long cycle_offset = 10000000000000ULL * (unsigned long long)cycle;
-  for (unsigned long long p = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; p < n;
-       p += (unsigned long long)gridDim.x * blockDim.x) {
+  for (unsigned long long p = bx * (unsigned long long)blockDim.x + threadIdx.x; p < n;
+       p += (unsigned long long)nbx * blockDim.x) {
     const uint32_t g = find_cell(c.off_new, m.n_cells, p);
     const unsigned long long local = p - c.off_new[g];
     double nodes[6], pos[3], dir[3];
@@ -172,6 +187,11 @@ __global__ void k_source_new(MeshDev m, CellsDev c, Bank b, const DeviceDiag *d,
   }
 }
 
+__global__ void k_source_new(MeshDev m, CellsDev c, Bank b, const DeviceDiag *d,
+                             unsigned long long seed_hi, uint32_t cycle, double dt) {
+  source_new_body(m, c, b, d, seed_hi, cycle, dt, blockIdx.x, gridDim.x);
+}
+
 void launch_plan_bank(const MeshDev &m, const CellsDev &c, DeviceDiag *d, uint32_t step,
                       unsigned long long capacity, cudaStream_t s) {
   k_plan_bank<<<1, 1, 0, s>>>(m, c, d, step, capacity);
@@ -182,6 +202,27 @@ void launch_source(const MeshDev &m, const CellsDev &c, const Bank &b, DeviceDia
   const unsigned long long seed_hi = (unsigned long long)seed << 32;
   if (step == 1) k_source_census<<<n_sm * 8, 256, 0, s>>>(m, c, b, d, seed_hi, dt);
   k_source_new<<<n_sm * 8, 256, 0, s>>>(m, c, b, d, seed_hi, step, dt);
+}
+
+// batched: problem blockIdx.y of the view table (plan, initial census at
+// step 1, then this step's photons)
+__global__ void k_b_plan_bank(const ProblemView *v) {
+  const ProblemView &P = v[blockIdx.y];
+  if (threadIdx.x == 0) plan_bank_body(P.m, P.c, P.d, P.step, P.capacity);
+}
+__global__ void __launch_bounds__(256) k_b_source_census(const ProblemView *v) {
+  const ProblemView &P = v[blockIdx.y];
+  if (P.step == 1) source_census_body(P.m, P.c, P.from, P.d, P.seed_hi, P.dt, blockIdx.x, gridDim.x);
+}
+__global__ void __launch_bounds__(256) k_b_source_new(const ProblemView *v) {
+  const ProblemView &P = v[blockIdx.y];
+  source_new_body(P.m, P.c, P.from, P.d, P.seed_hi, P.step, P.dt, blockIdx.x, gridDim.x);
+}
+
+void launch_batch_source(const ProblemView *v, const BatchGrid &g, cudaStream_t s) {
+  k_b_plan_bank<<<dim3(1, g.n), 32, 0, s>>>(v);
+  k_b_source_census<<<dim3(g.photons, g.n), 256, 0, s>>>(v);
+  k_b_source_new<<<dim3(g.photons, g.n), 256, 0, s>>>(v);
 }
 
 }  // namespace bgs

@@ -128,14 +128,15 @@ __global__ void __launch_bounds__(kTransportThreads, BGS_MIN_BLOCKS)
 __device__ __forceinline__ void block_sum128(unsigned long long lo, unsigned long long hi,
                                              unsigned long long *dst);
 
-__global__ void k_census(Bank from, Bank to, DeviceDiag *d, const unsigned long long *off,
-                         double next_dt) {
+__device__ __forceinline__ void census_body(const Bank &from, const Bank &to, DeviceDiag *d,
+                                            const unsigned long long *off, double next_dt, uint32_t bx,
+                                            uint32_t nbx) {
   const unsigned long long n = d->n_bank;
   const int sa = d->scale_abs;
   const double life = kC * next_dt;
   unsigned long long c_lo = 0, c_hi = 0, e_lo = 0, e_hi = 0;
-  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
-       i += (unsigned long long)gridDim.x * blockDim.x) {
+  for (unsigned long long i = bx * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+       i += (unsigned long long)nbx * blockDim.x) {
     const uint8_t desc = from.desc[i];
     unsigned long long lo, hi;
     if (desc == CENSUS) {
@@ -162,7 +163,11 @@ __global__ void k_census(Bank from, Bank to, DeviceDiag *d, const unsigned long 
   block_sum128(e_lo, e_hi, d->sum_exit);
 }
 
-__global__ void k_census_finish(DeviceDiag *d, const unsigned long long *off) {
+__global__ void k_census(Bank from, Bank to, DeviceDiag *d, const unsigned long long *off, double next_dt) {
+  census_body(from, to, d, off, next_dt, blockIdx.x, gridDim.x);
+}
+
+__device__ __forceinline__ void census_finish_body(DeviceDiag *d, const unsigned long long *off) {
   const unsigned long long n_out = off[d->n_bank];
   d->n_census_out = n_out;
   d->census_E = from_fixed128(d->sum_census[0], d->sum_census[1], d->scale_abs);
@@ -170,6 +175,18 @@ __global__ void k_census_finish(DeviceDiag *d, const unsigned long long *off) {
   // the census becomes the head of the next step's bank
   d->n_census_in = n_out;
   d->census_E_in = d->census_E;
+}
+
+__global__ void k_census_finish(DeviceDiag *d, const unsigned long long *off) { census_finish_body(d, off); }
+
+__global__ void __launch_bounds__(256) k_b_census(const ProblemView *v) {
+  const ProblemView &P = v[blockIdx.y];
+  census_body(P.from, P.to, P.d, P.off_bank, P.next_dt, blockIdx.x, gridDim.x);
+}
+
+__global__ void k_b_census_finish(const ProblemView *v) {
+  const ProblemView &P = v[blockIdx.y];
+  if (threadIdx.x == 0) census_finish_body(P.d, P.off_bank);
 }
 
 // 128-bit block sum via 43-bit limbs (exact for up to 2^21 terms per block)
@@ -226,6 +243,11 @@ void launch_census(const Bank &from, const Bank &to, DeviceDiag *d, const unsign
   cudaMemsetAsync(d->sum_exit, 0, sizeof(d->sum_exit), s);
   k_census<<<n_sm * 4, 256, 0, s>>>(from, to, d, off, next_dt);
   k_census_finish<<<1, 1, 0, s>>>(d, off);
+}
+
+void launch_batch_census(const ProblemView *v, const BatchGrid &g, cudaStream_t s) {
+  k_b_census<<<dim3(g.photons, g.n), 256, 0, s>>>(v);
+  k_b_census_finish<<<dim3(1, g.n), 32, 0, s>>>(v);
 }
 
 }  // namespace bgs

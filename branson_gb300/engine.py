@@ -246,3 +246,80 @@ def arrays_to_records(ph: PhotonArrays, dtype) -> np.ndarray:
     rec["stream"] = ph["rng_stream"]
     rec["counter"] = ph["rng_counter"]
     return rec
+
+
+class BatchIMC:
+    """Independent problems stepped together through bgs_batch_step: one
+    persistent transport launch over every problem's bank, the whole step
+    recorded as a CUDA graph.  ``problems[i]`` is an ordinary ReplicatedIMC;
+    read its results with its own calls."""
+
+    def __init__(self, decks, device: int = 0, capacities=None):
+        self.problems = [ReplicatedIMC(dk, device=device, capacity=None if capacities is None else capacities[i])
+                         for i, dk in enumerate(decks)]
+        self.lib = self.problems[0].lib
+        n = len(self.problems)
+        handles = (C.c_void_p * n)(*[p.ctx.value for p in self.problems])
+        h = C.c_void_p()
+        rc = self.lib.bgs_batch_create(C.byref(h), n, handles)
+        if rc != 0:
+            raise BransonError(rc, "bgs_batch_create")
+        self.handle = h
+
+    def _check(self, rc: int, what: str) -> None:
+        if rc != 0:
+            raise BransonError(rc, f"{what}: {self.lib.bgs_batch_last_error(self.handle).decode()}")
+
+    def step(self, sync: bool = True):
+        n = len(self.problems)
+        params = (_lib.StepParams * n)()
+        nds = []
+        for i, p in enumerate(self.problems):
+            nd = p.next_dt()
+            if nd <= 0.0:
+                nd = p.dt
+            nds.append(nd)
+            params[i] = _lib.StepParams(p.step_no, _lib.HISTORY, p.dt, nd)
+        out = (_lib.TransportDiag * n)() if sync else None
+        self._check(self.lib.bgs_batch_step(self.handle, params, out), "bgs_batch_step")
+        reps = None
+        if sync:
+            reps = [StepReport(p.step_no, p.dt, nds[i], o.n_transported, o.n_census, o.n_segments, o.census_E,
+                               o.exit_E, o.absorbed_E, o.post_mat_E, o.device_flags)
+                    for i, (p, o) in enumerate(zip(self.problems, out))]
+        for p, nd in zip(self.problems, nds):
+            p.advance_time(nd)
+        return reps
+
+    def synchronize(self) -> None:
+        self._check(self.lib.bgs_batch_synchronize(self.handle), "bgs_batch_synchronize")
+
+    def set_option(self, name: str, value: float) -> None:
+        self._check(self.lib.bgs_batch_set_option(self.handle, _lib.BATCH_OPTIONS[name], float(value)),
+                    "bgs_batch_set_option")
+
+    def last_transport_ms(self):
+        ms = C.c_float()
+        k = C.c_uint64()
+        self._check(self.lib.bgs_batch_last_transport_ms(self.handle, C.byref(ms), C.byref(k)),
+                    "bgs_batch_last_transport_ms")
+        return float(ms.value), int(k.value)
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.lib.bgs_batch_destroy(self.handle)
+            self.handle = None
+        for p in getattr(self, "problems", []):
+            p.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -269,6 +269,37 @@ BGS_API int bgs_adjoint_counts(const bgs_adjoint_tape *tape, uint32_t *counts);
 BGS_API int bgs_adjoint_get_info(const bgs_adjoint_tape *tape, bgs_adjoint_info *info);
 BGS_API int bgs_adjoint_release(bgs_adjoint_tape *tape);
 
+/* ------------------------------------------------------------ batching */
+/* No counterpart in the reference, which steps one problem per process.
+ * n independent problems, each an existing context (own mesh, deck, seed,
+ * photon count and bank), step together: per problem the energy,
+ * sourcing and transport-preparation phases run on the context's stream,
+ * one persistent launch then transports every problem's bank from a global
+ * work queue, and census compaction, tally reduce and temperature update
+ * follow per problem.  Each problem's results are those of bgs_step on its
+ * context alone.  By default the whole step is recorded as one CUDA graph
+ * (stream capture over the batch's and the contexts' streams) and launched
+ * with one call.  History mode only.  While a batch exists, its contexts
+ * must not be stepped or used on their own streams by other threads; the
+ * per-problem results are read with the usual per-context calls
+ * (bgs_get_cell_field, bgs_get_photons, ...).
+ *   params  n entries (step, BGS_HISTORY, dt, next_dt) per problem
+ *   out     n entries or NULL (NULL: the call returns without waiting) */
+typedef struct bgs_batch bgs_batch;
+enum {
+  BGS_BATCH_OPT_GRAPH = 0,            /* 1 (default): record each step as a CUDA graph; 0: plain launches */
+  BGS_BATCH_OPT_TRANSPORT_BLOCKS = 1  /* persistent-grid blocks of the batched launch (0: occupancy) */
+};
+BGS_API int bgs_batch_create(bgs_batch **batch, uint32_t n, bgs_context *const *contexts);
+BGS_API int bgs_batch_destroy(bgs_batch *batch);
+BGS_API const char *bgs_batch_last_error(const bgs_batch *batch);
+BGS_API int bgs_batch_step(bgs_batch *batch, const bgs_step_params *params, bgs_transport_diag *out);
+BGS_API int bgs_batch_synchronize(bgs_batch *batch);
+BGS_API int bgs_batch_set_option(bgs_batch *batch, int option, double value);
+/* Device time (ms) of the last batched transport launch, and the kernels
+ * the batch has launched (its own and the contexts' phases). */
+BGS_API int bgs_batch_last_transport_ms(bgs_batch *batch, float *ms, uint64_t *kernel_launches);
+
 /* ---------------------------------------------------------------- tuning */
 /* Execution options (the autotuner in branson_gb300/tune.py sets these; none
  * changes results, only how the work is scheduled).  No upstream counterpart:
