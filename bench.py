@@ -59,6 +59,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--cpu-photons", type=float, default=1e6)
     p.add_argument("--no-adjoint", action="store_true")
+    p.add_argument("--no-tune", action="store_true")
     p.add_argument("--no-batch", action="store_true")
     p.add_argument("--batch-problems", type=int, default=256)
     p.add_argument("--adjoint-photons", type=float, default=1e7)
@@ -232,6 +233,16 @@ def run_ours(args, rank, world, local):
             import torch.distributed as dist
             dist.barrier()
 
+    # the autotuner picks the transport schedule on this deck's first step
+    # (block size, histories per thread, history vs event mode; results are
+    # identical under every schedule)
+    tuning = None
+    if not args.no_tune:
+        from branson_gb300.tune import tune
+        res = tune(imc, repeats=2)
+        tuning = {"schedule": res.best.label(), "transport_ms": res.best_ms,
+                  "candidates": {c.label(): ms for c, ms in res.timings}}
+
     for _ in range(args.warmup):
         imc.step(sync=True)
     barrier()
@@ -313,7 +324,7 @@ def run_ours(args, rank, world, local):
                 "config": dict(cfg, parallelism=f"replicas{world}"), "roofline": roofline,
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
                 "segments_per_s": segs / elapsed * world, "histories_per_step": hist / args.steps,
-                "adjoint": adjoint, "batched": batched}
+                "tuning": tuning, "adjoint": adjoint, "batched": batched}
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist

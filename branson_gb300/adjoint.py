@@ -55,6 +55,36 @@ class Tape:
             pass
 
 
+def step_forward(imc: ReplicatedIMC, sigma_a: Optional[np.ndarray] = None, counts: Optional[np.ndarray] = None,
+                 tape: Optional[Tape] = None, save: bool = True, algorithm: int = _lib.HISTORY):
+    """bgs_adjoint_forward on any context: one step's sourcing and transport
+    at the context's current step number, the context left at that step;
+    returns (abs_E, tape) -- tape is None when save is False."""
+    n = imc.n_cells
+    sig = None if sigma_a is None else np.ascontiguousarray(sigma_a, dtype=np.float64)
+    if sig is not None and sig.shape != (n,):
+        raise ValueError("one sigma_a per cell")
+    cnt = None if counts is None else np.ascontiguousarray(counts, dtype=np.uint32)
+    if cnt is not None and cnt.shape != (3 * n,):
+        raise ValueError("3*n_cells photon counts (emission | source | initial census)")
+    nd = imc.next_dt()
+    if nd <= 0.0:
+        nd = imc.dt
+    p = _lib.StepParams(imc.step_no, algorithm, imc.dt, nd)
+    abs_E = np.empty(n)
+    h = C.c_void_p(tape.handle.value if tape is not None and tape.handle else None) if save else None
+    rc = imc.lib.bgs_adjoint_forward(imc.ctx, C.byref(p), _lib.ptr(sig), _lib.ptr(cnt), _lib.ptr(abs_E),
+                                     C.byref(h) if save else None)
+    imc._check(rc, "bgs_adjoint_forward")
+    if not save:
+        return abs_E, None
+    if tape is None:
+        tape = Tape(imc.lib, h, n)
+    else:
+        tape.handle = h
+    return abs_E, tape
+
+
 class AdjointStep(ReplicatedIMC):
     """A replicated IMC context whose current step can be run as a
     differentiable function sigma_a -> E_abs."""
@@ -63,29 +93,7 @@ class AdjointStep(ReplicatedIMC):
                 tape: Optional[Tape] = None, save: bool = True, algorithm: int = _lib.HISTORY):
         """One step's sourcing and transport at the current step number; returns
         (abs_E, tape) -- tape is None when save is False."""
-        n = self.n_cells
-        sig = None if sigma_a is None else np.ascontiguousarray(sigma_a, dtype=np.float64)
-        if sig is not None and sig.shape != (n,):
-            raise ValueError("one sigma_a per cell")
-        cnt = None if counts is None else np.ascontiguousarray(counts, dtype=np.uint32)
-        if cnt is not None and cnt.shape != (3 * n,):
-            raise ValueError("3*n_cells photon counts (emission | source | initial census)")
-        nd = self.next_dt()
-        if nd <= 0.0:
-            nd = self.dt
-        p = _lib.StepParams(self.step_no, algorithm, self.dt, nd)
-        abs_E = np.empty(n)
-        h = C.c_void_p(tape.handle.value if tape is not None and tape.handle else None) if save else None
-        rc = self.lib.bgs_adjoint_forward(self.ctx, C.byref(p), _lib.ptr(sig), _lib.ptr(cnt), _lib.ptr(abs_E),
-                                          C.byref(h) if save else None)
-        self._check(rc, "bgs_adjoint_forward")
-        if not save:
-            return abs_E, None
-        if tape is None:
-            tape = Tape(self.lib, h, n)
-        else:
-            tape.handle = h
-        return abs_E, tape
+        return step_forward(self, sigma_a, counts, tape, save, algorithm)
 
     def backward(self, tape: Tape, grad_abs_E: np.ndarray) -> np.ndarray:
         w = np.ascontiguousarray(grad_abs_E, dtype=np.float64)

@@ -616,8 +616,14 @@ int bgs_set_option(bgs_context *ctx, int option, double value) {
       return BGS_OK;
     case BGS_OPT_TRANSPORT_BLOCKS:
       if (!(value >= 0 && value <= 1e6)) break;
-      ctx->tshape = transport_launch_shape(ctx->n_sm);
+      ctx->transport_blocks = (int)value;
+      ctx->tshape = transport_launch_shape(ctx->n_sm, ctx->tshape.threads);
       if (value > 0) ctx->tshape.blocks = (int)value;
+      return BGS_OK;
+    case BGS_OPT_TRANSPORT_THREADS:
+      if (value != 64 && value != 128 && value != 256) break;
+      ctx->tshape = transport_launch_shape(ctx->n_sm, (int)value);
+      if (ctx->transport_blocks > 0) ctx->tshape.blocks = ctx->transport_blocks;
       return BGS_OK;
     default:
       return fail(ctx, BGS_ERR_INVALID, "unknown option %d", option);

@@ -59,6 +59,7 @@ struct bgs_context {
   DeviceDiag *d_diag = nullptr;
   DeviceDiag *h_diag = nullptr;  // pinned
   TransportLaunch tshape{};
+  int transport_blocks = 0;           // grid override of the history kernel (0: occupancy)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   uint32_t last_launches = 0;
   unsigned long long launches = 0;

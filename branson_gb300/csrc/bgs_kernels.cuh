@@ -98,7 +98,8 @@ void launch_source(const MeshDev &m, const CellsDev &c, const Bank &b, DeviceDia
 struct TransportLaunch {
   int blocks, threads;
 };
-TransportLaunch transport_launch_shape(int n_sm);
+// persistent grid of the history kernel for a block size of 64, 128 or 256
+TransportLaunch transport_launch_shape(int n_sm, int threads = 128);
 void launch_transport_history(const MeshDev &m, const CellsDev &c, const Bank &b, DeviceDiag *d,
                               uint32_t seed, const TransportLaunch &shape, cudaStream_t s);
 void launch_census(const Bank &from, const Bank &to, DeviceDiag *d, const unsigned long long *off,

@@ -21,9 +21,16 @@
 namespace bgs {
 
 // Work items: bank indices 0..n-1, or (kResume) the indices of an event-mode
-// active list, resumed with their carried per-cell tallies.
-template <bool kResume>
-__global__ void __launch_bounds__(kTransportThreads, BGS_MIN_BLOCKS)
+// active list, resumed with their carried per-cell tallies.  kThreads is the
+// block size (64, 128 or 256, chosen by the tuner); every size keeps the
+// register budget of BGS_MIN_BLOCKS blocks of 128 threads per SM.
+template <int kThreads>
+constexpr int min_blocks_for() {
+  return (BGS_MIN_BLOCKS * 128 / kThreads) > 0 ? (BGS_MIN_BLOCKS * 128 / kThreads) : 1;
+}
+
+template <bool kResume, int kThreads>
+__global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
     k_transport_history(MeshDev m, CellsDev c, Bank b, DeviceDiag *d, unsigned long long seed_hi,
                         EventState es) {
   const unsigned long long n = kResume ? (unsigned long long)*es.n_active : d->n_bank;
@@ -217,24 +224,50 @@ __device__ __forceinline__ void block_sum128(unsigned long long lo, unsigned lon
 }
 
 // ---------------------------------------------------------------------------
-TransportLaunch transport_launch_shape(int n_sm) {
+template <int kThreads>
+int history_blocks_per_sm() {
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_transport_history<false>, kTransportThreads, 0);
-  if (per_sm < 1) per_sm = 1;
-  return {n_sm * per_sm, kTransportThreads};
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_transport_history<false, kThreads>, kThreads, 0) !=
+          cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  return per_sm;
+}
+
+TransportLaunch transport_launch_shape(int n_sm, int threads) {
+  switch (threads) {
+    case 64: return {n_sm * history_blocks_per_sm<64>(), 64};
+    case 256: return {n_sm * history_blocks_per_sm<256>(), 256};
+    default: return {n_sm * history_blocks_per_sm<128>(), 128};
+  }
+}
+
+template <bool kResume>
+void launch_history_kernel(const MeshDev &m, const CellsDev &c, const Bank &b, DeviceDiag *d,
+                           unsigned long long seed_hi, const EventState &es, const TransportLaunch &shape,
+                           cudaStream_t s) {
+  switch (shape.threads) {
+    case 64:
+      k_transport_history<kResume, 64><<<shape.blocks, 64, 0, s>>>(m, c, b, d, seed_hi, es);
+      break;
+    case 256:
+      k_transport_history<kResume, 256><<<shape.blocks, 256, 0, s>>>(m, c, b, d, seed_hi, es);
+      break;
+    default:
+      k_transport_history<kResume, 128><<<shape.blocks, 128, 0, s>>>(m, c, b, d, seed_hi, es);
+      break;
+  }
 }
 
 void launch_transport_history(const MeshDev &m, const CellsDev &c, const Bank &b, DeviceDiag *d,
                               uint32_t seed, const TransportLaunch &shape, cudaStream_t s) {
-  const unsigned long long seed_hi = (unsigned long long)seed << 32;
-  k_transport_history<false><<<shape.blocks, shape.threads, 0, s>>>(m, c, b, d, seed_hi, EventState{});
+  launch_history_kernel<false>(m, c, b, d, (unsigned long long)seed << 32, EventState{}, shape, s);
 }
 
 void launch_transport_resume(const MeshDev &m, const CellsDev &c, const Bank &b, DeviceDiag *d,
                              uint32_t seed, const EventState &es, const TransportLaunch &shape,
                              cudaStream_t s) {
-  const unsigned long long seed_hi = (unsigned long long)seed << 32;
-  k_transport_history<true><<<shape.blocks, shape.threads, 0, s>>>(m, c, b, d, seed_hi, es);
+  launch_history_kernel<true>(m, c, b, d, (unsigned long long)seed << 32, es, shape, s);
 }
 
 void launch_census(const Bank &from, const Bank &to, DeviceDiag *d, const unsigned long long *off,

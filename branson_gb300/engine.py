@@ -48,6 +48,7 @@ class ReplicatedIMC:
                  stream: Optional[int] = None):
         self.lib = _lib.load()
         self.deck = deck
+        self.device = device
         deck.validate()
         self.capacity = int(capacity or default_capacity(deck))
         ctx = C.c_void_p()

@@ -308,7 +308,9 @@ enum {
   BGS_OPT_EVENT_ROUND_CAP = 0,      /* event rounds before the tail goes to the history kernel */
   BGS_OPT_EVENT_CHECK_EVERY = 1,    /* rounds between host reads of the active count */
   BGS_OPT_EVENT_TAIL_FRACTION = 2,  /* active share below which event rounds stop */
-  BGS_OPT_TRANSPORT_BLOCKS = 3      /* persistent-grid blocks for the history kernel (0: occupancy) */
+  BGS_OPT_TRANSPORT_BLOCKS = 3,     /* persistent-grid blocks for the history kernel (0: occupancy);
+                                       histories per thread = histories / (blocks * threads) */
+  BGS_OPT_TRANSPORT_THREADS = 4     /* block size of the history kernel: 64, 128 (default) or 256 */
 };
 BGS_API int bgs_set_option(bgs_context *ctx, int option, double value);
 
