@@ -224,7 +224,8 @@ def run_ours(args, rank, world, local):
     from branson_gb300.engine import ReplicatedIMC, records_to_arrays
 
     dk, cfg = make_deck(args)
-    dk.seed = (dk.seed + 7919 * rank) & 0xFFFFFFFF  # independent replica per rank
+    from branson_gb300.replicas import combine, replica_seed
+    dk.seed = replica_seed(dk.seed, rank)  # independent replica per rank
     stream = torch.cuda.Stream(device=dev)
     imc = ReplicatedIMC(dk, device=dev, stream=stream.cuda_stream)
 
@@ -268,16 +269,7 @@ def run_ours(args, rank, world, local):
     elapsed = ev0.elapsed_time(ev1) / 1e3
     launches = imc.kernel_launches() - launches0
     clk = clocks.stop()
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([elapsed], device=f"cuda:{dev}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
-        h = torch.tensor([float(hist)], device=f"cuda:{dev}")
-        dist.all_reduce(h)
-        hist_all = float(h.item())
-    else:
-        hist_all = float(hist)
+    elapsed, hist_all = combine(elapsed, hist, device=f"cuda:{dev}")
     value = hist_all / elapsed
 
     # roofline of the dominant kernel (k_transport_history), live CUDA events
