@@ -62,6 +62,10 @@ def parse():
     p.add_argument("--no-tune", action="store_true")
     p.add_argument("--no-batch", action="store_true")
     p.add_argument("--batch-problems", type=int, default=256)
+    p.add_argument("--batch-photon-scale", type=float, default=1.0,
+                   help="scale of the ensemble's photon counts (profiling small cases)")
+    p.add_argument("--only", choices=["main", "adjoint", "batch"], default=None,
+                   help="run one section alone and print its JSON (profiling)")
     p.add_argument("--adjoint-photons", type=float, default=1e7)
     return p.parse_args()
 
@@ -369,7 +373,9 @@ def batch_bench(args, dev, steps: int = 2):
     from branson_gb300.engine import BatchIMC, ReplicatedIMC
 
     n = args.batch_problems
-    decks = D.batch_ensemble(n_problems=n, master_seed=777)
+    k = args.batch_photon_scale
+    decks = D.batch_ensemble(n_problems=n, master_seed=777, photon_median=1e5 * k,
+                             photon_range=(max(1, int(1e4 * k)), max(1, int(1e6 * k))))
     # warm-up of the batched path (module load, graph machinery) on a small ensemble
     with BatchIMC(D.batch_ensemble(n_problems=4, master_seed=1, side_range=(4, 8), photon_median=2000,
                                    photon_range=(1000, 4000)), device=dev) as w:
@@ -404,8 +410,8 @@ def batch_bench(args, dev, steps: int = 2):
     assert seq["hist"] == bat["hist"] and seq["seg"] == bat["seg"], "batched and sequential runs disagree"
     rate_s = sum(seq["hist"]) / sum(seq["s"])
     rate_b = sum(bat["hist"]) / sum(bat["s"])
-    return {"workload": f"batch_ensemble of {n} problems (side U{{8..64}}, photons lognormal median 1e5 in "
-                        "[1e4, 1e6], sigma_a U(1,200), T_source U(0.2,1)), steps from step 1",
+    return {"workload": f"batch_ensemble of {n} problems (side U{{8..64}}, photons lognormal median {1e5 * k:g} in "
+                        f"[{1e4 * k:g}, {1e6 * k:g}], sigma_a U(1,200), T_source U(0.2,1)), steps from step 1",
             "steps": steps, "histories_per_step": seq["hist"], "segments_per_step": seq["seg"],
             "sequential_hist_per_s": rate_s, "batched_hist_per_s": rate_b, "batched_over_sequential": rate_b / rate_s,
             "sequential_step_s": seq["s"], "batched_step_s": bat["s"],
@@ -517,6 +523,14 @@ def adjoint_bench(args, dev, replicas: int = 6):
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.only in ("adjoint", "batch"):
+        import torch
+        torch.cuda.set_device(0)
+        sect = adjoint_bench(args, 0) if args.only == "adjoint" else batch_bench(args, 0)
+        print(json.dumps({"section": args.only, args.only: sect}), flush=True)
+        return
+    if args.only == "main":
+        args.no_adjoint = args.no_batch = True
     if args.impl == "reference":
         run_reference(args, rank, world)
         return
