@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(kAdjThreads, BGS_ADJ_MIN_BLOCKS)
           L.rng.stream = t.stream[i]; L.rng.ctr = t.ctr[i]; L.rng.hi = seed_hi;
           L.segs = 0;
           L.thr_abs = 0.0; L.thr_trk = 0.0;
-          L.inv_E0 = 1.0 / L.E0;
+          L.kill_thr = kCutoff * L.E0;
           direction_recips(L);
           prefix = 0.0; vis_a = 0.0; vis_b = 0.0;
           n_log = 0;

@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(kTransportThreads, BGS_MIN_BLOCKS)
           L.rng.stream = b.stream[i]; L.rng.ctr = b.ctr[i]; L.rng.hi = P.seed_hi;
           L.segs = 0;
           L.thr_abs = 0.0; L.thr_trk = 0.0;
-          L.inv_E0 = 1.0 / L.E0;
+          L.kill_thr = kCutoff * L.E0;
           direction_recips(L);
           xs_p = P.c.xs;
           if (L.cell < P.m.n_cells) {

@@ -39,7 +39,7 @@ __device__ __forceinline__ void load_lane(const MeshDev &m, const Bank &b, const
   L.rng.stream = b.stream[p]; L.rng.ctr = b.ctr[p]; L.rng.hi = seed_hi;
   L.thr_abs = first ? 0.0 : es.thr_abs[p];
   L.thr_trk = first ? 0.0 : es.thr_trk[p];
-  L.inv_E0 = 1.0 / L.E0;
+  L.kill_thr = kCutoff * L.E0;
   L.segs = 0;
   direction_recips(L);
   locate(m, L);

@@ -51,11 +51,15 @@ constexpr uint32_t kMaxSegmentsPerHistory = 100000000u;
 //                                          contribution absorbed/(sigma_a f) is
 //                                          formed as a product, within 1 ulp)
 //   p_scat   = sigma_s / sig_eff           (physical-scatter probability)
+//   inv_se   = RN(1/sig_eff) for the correctly rounded division
+//              -log(u)/sig_eff by one multiply and two fma (div_recip in
+//              bgs_physics.cuh); 0 if sig_eff is 0 or out of that range
 //   rb_sig   = 64-bit reciprocal of sig_eff's mantissa for the exact integer
 //              division -log(u)/sig_eff (bgs_fixmath.cuh div_rn)
 struct __align__(16) CellXS {
   double sig_eff, neg_saf, inv_saf, p_scat;
-  unsigned long long rb_sig, pad;
+  unsigned long long rb_sig;
+  double inv_se;
 };
 
 // 128-bit fixed-point tally cell: value = (hi*2^64 + lo) * 2^-scale.

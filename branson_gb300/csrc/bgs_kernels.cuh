@@ -50,6 +50,13 @@ __device__ __forceinline__ double pow_deck(double x, double c) {
   return pow(x, c);
 }
 
+// RN(1/b) for div_recip (bgs_physics.cuh), or 0 when |b| is outside
+// [2^-900, 2^900], where the division must be done directly
+__device__ __forceinline__ double recip_for_div(double b) {
+  const double ab = fabs(b);
+  return (ab >= 0x1p-900 && ab <= 0x1p900) ? 1.0 / b : 0.0;
+}
+
 // per-cell transport coefficients (see CellXS) and the CDF step of
 // sample_emission_group's walk, op_a(g) * 1/(op_a(0)*N) with all groups
 // equal (sampling_functions.h:132-135, cell.h:260-266)
@@ -61,7 +68,7 @@ __device__ __forceinline__ void set_cell_xs(const CellsDev &c, uint32_t g, doubl
   x.inv_saf = 1.0 / (op_a * f);
   x.p_scat = op_s / ((1.0 - f) * op_a + op_s);
   x.rb_sig = x.sig_eff > 0.0 ? fix::divisor_recip(x.sig_eff) : 0ULL;
-  x.pad = 0;
+  x.inv_se = recip_for_div(x.sig_eff);
   c.xs[g] = x;
   const double norm_factor = 1.0 / (op_a * (double)n_groups);
   c.group_v[g] = op_a * norm_factor;

@@ -27,10 +27,39 @@ constexpr int kTransportThreads = 128;
 #ifndef BGS_INT_DIV_DS
 #define BGS_INT_DIV_DS 0  // -log(u)/sigma_eff by the exact integer division (per-cell reciprocal)
 #endif
+#ifndef BGS_RECIP_DIV
+#define BGS_RECIP_DIV 0   // face distances: division by the direction's stored reciprocals (div_recip)
+#endif
+#ifndef BGS_RECIP_DIV_DS
+#define BGS_RECIP_DIV_DS 1  // -log(u)/sigma_eff: division by the cell's stored reciprocal
+#endif
 
-__device__ __forceinline__ double seg_div(double a, double b, unsigned long long rb) {
+// a/b correctly rounded from y = RN(1/b): q0 = RN(a*y) is within one ulp of
+// a/b, the remainder a - b*q0 is exact in one fma, and RN(q0 + r*y) is the
+// correctly rounded quotient (Markstein's theorem for round-to-nearest, no
+// overflow or underflow in the steps: |b| in [2^-900, 2^900] and |a| far
+// below 2^100 here).  Three FP64 operations instead of a division; y == 0
+// marks a divisor outside that range, which is divided directly.  The
+// result equals the IEEE quotient a/b bit for bit (also checked against it
+// on 1e9 random and adversarial operand pairs).
+__device__ __forceinline__ double div_recip(double a, double b, double y) {
+  if (__double_as_longlong(y) == 0) return a / b;
+  const double q0 = __dmul_rn(a, y);
+  const double r = __fma_rn(-q0, b, a);
+  return __fma_rn(r, y, q0);
+}
+
+#if BGS_INT_DIV
+using DivRecip = unsigned long long;  // fix::divisor_recip of the direction cosine
+#else
+using DivRecip = double;              // RN(1/direction cosine) (recip_for_div)
+#endif
+
+__device__ __forceinline__ double seg_div(double a, double b, DivRecip rb) {
 #if BGS_INT_DIV
   return fix::div_rn(a, b, rb);
+#elif BGS_RECIP_DIV
+  return div_recip(a, b, rb);
 #else
   (void)rb;
   return a / b;
@@ -52,8 +81,9 @@ __device__ __forceinline__ void seg_sincos(double phi, double *s, double *c) {
 }
 
 struct Lane {
-  double px, py, pz, dx, dy, dz, E, E0, life, inv_E0;
-  unsigned long long rbx, rby, rbz;  // divisor reciprocals of the direction cosines
+  double px, py, pz, dx, dy, dz, E, E0, life;
+  double kill_thr;  // RN(0.01 * E0): the cutoff test runs against it in integer ulps
+  DivRecip rbx, rby, rbz;  // divisor reciprocals of the direction cosines
   double n0, n1, n2, n3, n4, n5;  // nodes of the current cell
   double thr_abs, thr_trk;
   unsigned long long idx;
@@ -82,11 +112,14 @@ __device__ __forceinline__ void flush_tally(const CellsDev &c, const DeviceDiag 
 }
 
 __device__ __forceinline__ void direction_recips(Lane &L) {
-
 #if BGS_INT_DIV
   L.rbx = fix::divisor_recip(L.dx);
   L.rby = fix::divisor_recip(L.dy);
   L.rbz = fix::divisor_recip(L.dz);
+#elif BGS_RECIP_DIV
+  L.rbx = recip_for_div(L.dx);
+  L.rby = recip_for_div(L.dy);
+  L.rbz = recip_for_div(L.dz);
 #else
   (void)L;
 #endif
@@ -116,6 +149,19 @@ __device__ __forceinline__ uint32_t sample_group(Rng &r, double v, uint32_t n_gr
 }
 
 
+// Comparisons on the integer pipe.  FP64 issue is the transport kernels'
+// bound on this part (two FP64 lanes per clock per SM), so the segment's
+// ordering tests use the doubles' bit patterns: for any non-NaN a and b,
+// a < b exactly when f64_key(a) < f64_key(b) (the key is monotone over the
+// signed 64-bit integers and gives -0 and +0 the same value), and
+// f64_positive(x) is 0.0 < x.
+__device__ __forceinline__ long long f64_key(double x) {
+  long long b = __double_as_longlong(x);
+  if (b == (long long)0x8000000000000000ULL) b = 0;  // -0 orders as +0
+  return b >= 0 ? b : (b ^ 0x7FFFFFFFFFFFFFFFLL);
+}
+__device__ __forceinline__ bool f64_positive(double x) { return __double_as_longlong(x) > 0; }
+
 // what one segment ends in (the event branches of transport_photon)
 enum SegEvent : int { SEG_KILLED = 0, SEG_SCATTER = 1, SEG_BOUNDARY = 2, SEG_CENSUS = 3 };
 
@@ -134,34 +180,44 @@ struct SegInfo {
 __device__ __forceinline__ int segment_advance(const CellXS &xs, Lane &L, uint32_t &surface_cross,
                                                uint32_t &flags, SegInfo *info = nullptr) {
   ++L.segs;
+  const bool scatters = f64_positive(xs.sig_eff);
 #if BGS_INT_DIV_DS
   const double dist_to_scatter =
-      (xs.sig_eff > 0.0) ? fix::div_rn(fix::neg_log_u53(L.rng.next_m53()), xs.sig_eff, xs.rb_sig)
-                         : 1.0e100;
+      scatters ? fix::div_rn(fix::neg_log_u53(L.rng.next_m53()), xs.sig_eff, xs.rb_sig) : 1.0e100;
+#elif BGS_RECIP_DIV_DS
+  // -log(u) / sigma_eff with the integer, correctly rounded -log
+  // (bgs_fixmath.cuh) and the division by the cell's stored reciprocal
+  const double dist_to_scatter =
+      scatters ? div_recip(fix::neg_log_u53(L.rng.next_m53()), xs.sig_eff, xs.inv_se) : 1.0e100;
 #else
   // -log(u) / sigma_eff with the integer, correctly rounded -log (bgs_fixmath.cuh)
-  const double dist_to_scatter =
-      (xs.sig_eff > 0.0) ? fix::neg_log_u53(L.rng.next_m53()) / xs.sig_eff : 1.0e100;
+  const double dist_to_scatter = scatters ? fix::neg_log_u53(L.rng.next_m53()) / xs.sig_eff : 1.0e100;
 #endif
-  // Cell::get_distance_to_boundary (cell.h:117-132)
+  // Cell::get_distance_to_boundary (cell.h:117-132); the comparisons are
+  // the upstream ones, evaluated on the integer keys
   double dist_to_boundary = 1.0e16;
+  long long k_boundary = f64_key(1.0e16);
   surface_cross = 0;
-  const bool posx = 0.0 < L.dx, posy = 0.0 < L.dy, posz = 0.0 < L.dz;
+  const bool posx = f64_positive(L.dx), posy = f64_positive(L.dy), posz = f64_positive(L.dz);
   {
     double dist = seg_div((posx ? L.n1 : L.n0) - L.px, L.dx, L.rbx);
-    if (dist < dist_to_boundary) { dist_to_boundary = dist; surface_cross = posx ? 1u : 0u; }
+    long long k = f64_key(dist);
+    if (k < k_boundary) { dist_to_boundary = dist; k_boundary = k; surface_cross = posx ? 1u : 0u; }
     dist = seg_div((posy ? L.n3 : L.n2) - L.py, L.dy, L.rby);
-    if (dist < dist_to_boundary) { dist_to_boundary = dist; surface_cross = posy ? 3u : 2u; }
+    k = f64_key(dist);
+    if (k < k_boundary) { dist_to_boundary = dist; k_boundary = k; surface_cross = posy ? 3u : 2u; }
     dist = seg_div((posz ? L.n5 : L.n4) - L.pz, L.dz, L.rbz);
-    if (dist < dist_to_boundary) { dist_to_boundary = dist; surface_cross = posz ? 5u : 4u; }
+    k = f64_key(dist);
+    if (k < k_boundary) { dist_to_boundary = dist; k_boundary = k; surface_cross = posz ? 5u : 4u; }
   }
   const double dist_to_census = L.life;
   // std::min(a, b) == (b < a) ? b : a; the event tests that follow
   // (dist_to_event == dist_to_scatter, then == dist_to_boundary) are the
   // same comparisons read back
-  const bool census_first = dist_to_census < dist_to_boundary;
+  const long long k_census = f64_key(dist_to_census);
+  const bool census_first = k_census < k_boundary;
   const double inner = census_first ? dist_to_census : dist_to_boundary;
-  const bool inner_first = inner < dist_to_scatter;
+  const bool inner_first = (census_first ? k_census : k_boundary) < f64_key(dist_to_scatter);
   const double dist_to_event = inner_first ? inner : dist_to_scatter;
 
   const double absorbed_E = L.E * (1.0 - fix::exp_neg(-(xs.neg_saf * dist_to_event)));
@@ -178,11 +234,12 @@ __device__ __forceinline__ int segment_advance(const CellXS &xs, Lane &L, uint32
     info->collided = !inner_first;
   }
 
-  // below_cutoff: E/E0 < 0.01 (photon.h:47-49), decided from E*(1/E0) and
-  // settled with the exact quotient only within a few ulps of the threshold
-  const double frac = L.E * L.inv_E0;
-  bool killed = frac < kCutoff;
-  if (fabs(frac - kCutoff) <= 4.0e-18) killed = L.E / L.E0 < kCutoff;
+  // below_cutoff: E/E0 < 0.01 (photon.h:47-49).  More than four ulps from
+  // RN(0.01*E0), E < RN(0.01*E0) decides it the same way as RN(E/E0) < 0.01;
+  // closer than that the exact quotient settles it
+  const long long k_e = f64_key(L.E), k_thr = f64_key(L.kill_thr);
+  bool killed = k_e < k_thr;
+  if (k_e - k_thr <= 4 && k_thr - k_e <= 4) killed = L.E / L.E0 < kCutoff;
   if (killed || L.segs >= kMaxSegmentsPerHistory) {
     if (!killed) flags |= FLAG_SEGMENT_LIMIT;
     L.thr_abs += L.E;
@@ -247,12 +304,25 @@ __device__ __forceinline__ void enter_neighbour(const MeshDev &m, Lane &L, uint3
   load_nodes(m, L);
 }
 
-// REFLECT: Photon::reflect (photon.h:151-155); the reciprocals depend only on
-// the magnitudes, so they are unchanged
+// REFLECT: Photon::reflect (photon.h:151-155).  An integer divisor
+// reciprocal depends only on the magnitude; RN(1/-b) = -RN(1/b) exactly.
 __device__ __forceinline__ void reflect(Lane &L, uint32_t surface_cross) {
-  if (surface_cross < 2) L.dx = -L.dx;
-  else if (surface_cross < 4) L.dy = -L.dy;
-  else L.dz = -L.dz;
+  if (surface_cross < 2) {
+    L.dx = -L.dx;
+#if !BGS_INT_DIV
+    L.rbx = -L.rbx;
+#endif
+  } else if (surface_cross < 4) {
+    L.dy = -L.dy;
+#if !BGS_INT_DIV
+    L.rby = -L.rby;
+#endif
+  } else {
+    L.dz = -L.dz;
+#if !BGS_INT_DIV
+    L.rbz = -L.rbz;
+#endif
+  }
 }
 
 // cell coordinates and nodes from the global cell index

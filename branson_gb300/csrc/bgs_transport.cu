@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
           } else {
             L.thr_abs = 0.0; L.thr_trk = 0.0;
           }
-          L.inv_E0 = 1.0 / L.E0;
+          L.kill_thr = kCutoff * L.E0;
           direction_recips(L);
           if (L.cell < m.n_cells) {
             locate(m, L);

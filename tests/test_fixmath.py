@@ -162,3 +162,18 @@ def test_sqrt_matches_ieee_bitwise():
                         [1.0, 0.25, np.nextafter(1.0, 0), 2.0 ** -51, 3.0, 4.0, np.nextafter(4.0, 0)]])
     got = np.array([L.fix_sqrt(v) for v in x])
     assert np.array_equal(got.view(np.int64), np.sqrt(x).view(np.int64))
+
+
+def test_division_by_stored_reciprocal_is_ieee(tmp_path):
+    """The transport kernels divide by a stored reciprocal with two fma
+    (Markstein's final step); the quotient must be the IEEE one bit for bit."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc")
+    if cc is None:
+        pytest.skip("gcc not available")
+    src = os.path.join(os.path.dirname(__file__), "div_recip_check.c")
+    exe = str(tmp_path / "div_recip_check")
+    subprocess.run([cc, "-O2", "-std=c11", "-ffp-contract=off", "-o", exe, src, "-lm"], check=True)
+    r = subprocess.run([exe, "3000000"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout
