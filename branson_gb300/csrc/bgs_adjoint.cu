@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(kAdjThreads, BGS_ADJ_MIN_BLOCKS)
           L.cell = t.cell[i]; L.group = t.group[i];
           L.rng.stream = t.stream[i]; L.rng.ctr = t.ctr[i]; L.rng.hi = seed_hi;
           L.segs = 0;
-          L.thr_abs = 0.0; L.thr_trk = 0.0;
+          L.thr_abs = 0.0;
           L.kill_thr = kCutoff * L.E0;
           direction_recips(L);
           prefix = 0.0; vis_a = 0.0; vis_b = 0.0;
@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(kAdjThreads, BGS_ADJ_MIN_BLOCKS)
       const int bc = face_bc(m, L, surface_cross);
       if (bc == ELEMENT) leave = true;
       else if (bc == VACUUM || bc == SOURCE || bc == PROCESSOR) end = true;
-      else reflect(L, surface_cross);
+      else reflect(m, L, surface_cross);
     }
     if (leave || end) {  // the visit to this cell is over
       if (kPass == 0) {

@@ -348,7 +348,7 @@ int ensure_event_state(bgs_context *ctx) {
   EventState e{};
   int rc;
   auto &L = ctx->event_allocs;
-  if ((rc = dev_alloc(ctx, L, &e.thr_abs, cap)) || (rc = dev_alloc(ctx, L, &e.thr_trk, cap)) ||
+  if ((rc = dev_alloc(ctx, L, &e.thr_abs, cap)) ||
       (rc = dev_alloc(ctx, L, &e.surface, cap)) || (rc = dev_alloc(ctx, L, &e.active, cap)) ||
       (rc = dev_alloc(ctx, L, &e.next, cap)) || (rc = dev_alloc(ctx, L, &e.q_scatter, cap)) ||
       (rc = dev_alloc(ctx, L, &e.q_boundary, cap)))

@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(kTransportThreads, BGS_MIN_BLOCKS)
           L.cell = b.cell[i]; L.group = b.group[i];
           L.rng.stream = b.stream[i]; L.rng.ctr = b.ctr[i]; L.rng.hi = P.seed_hi;
           L.segs = 0;
-          L.thr_abs = 0.0; L.thr_trk = 0.0;
+          L.thr_abs = 0.0;
           L.kill_thr = kCutoff * L.E0;
           direction_recips(L);
           xs_p = P.c.xs;
@@ -153,15 +153,14 @@ __global__ void __launch_bounds__(kTransportThreads, BGS_MIN_BLOCKS)
       const MeshDev &m = probs[p].m;
       const int bc = face_bc(m, L, surface_cross);
       if (bc == ELEMENT) {
-        flush_batched(probs[p], L.cell, L.thr_abs, L.thr_trk, flags);
+        flush_batched(probs[p], L.cell, L.thr_abs, visit_track(xs, L, ev), flags);
         L.thr_abs = 0.0;
-        L.thr_trk = 0.0;
         enter_neighbour(m, L, surface_cross);
       } else if (bc == VACUUM || bc == SOURCE || bc == PROCESSOR) {
         end = true;
         desc = bc == PROCESSOR ? PASS : EXIT;
       } else {
-        reflect(L, surface_cross);
+        reflect(m, L, surface_cross);
       }
     } else {  // SEG_CENSUS
       end = true;
@@ -169,7 +168,7 @@ __global__ void __launch_bounds__(kTransportThreads, BGS_MIN_BLOCKS)
     }
     if (end) {
       const ProblemView &P = probs[p];
-      flush_batched(P, L.cell, L.thr_abs, L.thr_trk, flags);
+      flush_batched(P, L.cell, L.thr_abs, visit_track(xs, L, ev), flags);
       store_end(P.from, L, desc);
       atomicAdd(&P.d->n_segments, (unsigned long long)L.segs);
       if (flags) {

@@ -38,7 +38,6 @@ __device__ __forceinline__ void load_lane(const MeshDev &m, const Bank &b, const
   L.cell = b.cell[p]; L.group = b.group[p];
   L.rng.stream = b.stream[p]; L.rng.ctr = b.ctr[p]; L.rng.hi = seed_hi;
   L.thr_abs = first ? 0.0 : es.thr_abs[p];
-  L.thr_trk = first ? 0.0 : es.thr_trk[p];
   L.kill_thr = kCutoff * L.E0;
   L.segs = 0;
   direction_recips(L);
@@ -85,12 +84,12 @@ __global__ void __launch_bounds__(kEventThreads) k_event_advance(MeshDev m, Cell
         const CellXS xs = c.xs[L.cell];
         ev = segment_advance(xs, L, sc, flags);
         if (ev == SEG_KILLED || ev == SEG_CENSUS) {
-          flush_tally(c, d, L.cell, L.thr_abs, L.thr_trk, flags, sa, st);
+          flush_tally(c, d, L.cell, L.thr_abs, visit_track(xs, L, ev), flags, sa, st);
           store_end(b, L, ev == SEG_KILLED ? KILLED : CENSUS);
         } else {
           b.px[p] = L.px; b.py[p] = L.py; b.pz[p] = L.pz;
           b.E[p] = L.E; b.life[p] = L.life; b.ctr[p] = L.rng.ctr;
-          es.thr_abs[p] = L.thr_abs; es.thr_trk[p] = L.thr_trk;
+          es.thr_abs[p] = L.thr_abs;
           if (ev == SEG_BOUNDARY) es.surface[p] = (uint8_t)sc;
         }
       }
@@ -153,9 +152,9 @@ __global__ void __launch_bounds__(kEventThreads) k_event_boundary(MeshDev m, Cel
       const uint32_t sc = es.surface[p];
       const int bc = face_bc(m, L, sc);
       if (bc == ELEMENT) {
-        flush_tally(c, d, L.cell, es.thr_abs[p], es.thr_trk[p], flags, sa, st);
+        const double a = es.thr_abs[p];
+        flush_tally(c, d, L.cell, a, a * c.xs[L.cell].inv_saf, flags, sa, st);
         es.thr_abs[p] = 0.0;
-        es.thr_trk[p] = 0.0;
         switch (sc) {
           case 0: L.cell -= 1; break;
           case 1: L.cell += 1; break;
@@ -167,7 +166,8 @@ __global__ void __launch_bounds__(kEventThreads) k_event_boundary(MeshDev m, Cel
         b.cell[p] = L.cell;
         survive = true;
       } else if (bc == VACUUM || bc == SOURCE || bc == PROCESSOR) {
-        flush_tally(c, d, L.cell, es.thr_abs[p], es.thr_trk[p], flags, sa, st);
+        const double a = es.thr_abs[p];
+        flush_tally(c, d, L.cell, a, a * c.xs[L.cell].inv_saf, flags, sa, st);
         b.desc[p] = bc == PROCESSOR ? PASS : EXIT;
       } else {  // REFLECT (photon.h:151-155)
         if (sc < 2) b.dx[p] = -b.dx[p];

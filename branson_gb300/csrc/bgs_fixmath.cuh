@@ -190,7 +190,8 @@ BGS_HD double exp_neg(double tau) {
   const uint64_t tb = double_to_bits(tau);
   const int te = (int)((tb >> 52) & 0x7FF);
   if (te == 0) return 1.0;  // tau = 0 (or subnormal: exp rounds to 1)
-  if (!(tau <= 700.0)) return tau == tau ? exp(-tau) : tau;
+  // tau > 700 (or a NaN) by the bit pattern: 700.0 is 0x4085E00000000000
+  if (tb > 0x4085E00000000000ULL) return tau == tau ? exp(-tau) : tau;
   // T = tau * 2^96 as a 128-bit integer (truncating below 2^-96)
   const uint64_t tm = (tb & 0x000FFFFFFFFFFFFFULL) | 0x0010000000000000ULL;
   const int sh = te - 1075 + 96;  // tau = tm * 2^(te-1075)
@@ -246,7 +247,9 @@ BGS_HD void sincos_phi(double phi, double *s_out, double *c_out) {
   constexpr uint64_t kCo[10] = {BGS_COS_COEF_INIT};
   const uint64_t pb = double_to_bits(phi);
   const int be = (int)((pb >> 52) & 0x7FF);
-  if (be == 0 || !(phi < 8.0) || !(phi > 0.0)) {
+  // 0 < phi < 8 by the bit pattern (8.0 is 0x4020000000000000; a set sign
+  // bit, a NaN or a zero/subnormal exponent all fall outside)
+  if (be == 0 || pb >= 0x4020000000000000ULL) {
 #if defined(__CUDA_ARCH__)
     sincos(phi, s_out, c_out);
 #else

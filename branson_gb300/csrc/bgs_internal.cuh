@@ -98,7 +98,7 @@ struct CellsDev {
 // Event-mode state: per-photon carried tallies and surface, the active list
 // and the per-event queues (indices into the bank), with device counters.
 struct EventState {
-  double *thr_abs, *thr_trk;   // per-cell-visit tallies carried between stages
+  double *thr_abs;             // per-cell-visit absorbed energy carried between stages
   uint8_t *surface;            // face crossed by a boundary event
   uint32_t *active, *next, *q_scatter, *q_boundary;
   unsigned int *n_active, *n_next, *n_scatter, *n_boundary;  // device counters

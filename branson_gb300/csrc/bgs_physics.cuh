@@ -22,7 +22,7 @@ constexpr int kTransportThreads = 128;
 #define BGS_INT_SINCOS 1
 #endif
 #ifndef BGS_MIN_BLOCKS
-#define BGS_MIN_BLOCKS 5
+#define BGS_MIN_BLOCKS 6
 #endif
 #ifndef BGS_INT_DIV_DS
 #define BGS_INT_DIV_DS 0  // -log(u)/sigma_eff by the exact integer division (per-cell reciprocal)
@@ -33,6 +33,7 @@ constexpr int kTransportThreads = 128;
 #ifndef BGS_RECIP_DIV_DS
 #define BGS_RECIP_DIV_DS 1  // -log(u)/sigma_eff: division by the cell's stored reciprocal
 #endif
+
 
 // a/b correctly rounded from y = RN(1/b): q0 = RN(a*y) is within one ulp of
 // a/b, the remainder a - b*q0 is exact in one fma, and RN(q0 + r*y) is the
@@ -84,28 +85,33 @@ struct Lane {
   double px, py, pz, dx, dy, dz, E, E0, life;
   double kill_thr;  // RN(0.01 * E0): the cutoff test runs against it in integer ulps
   DivRecip rbx, rby, rbz;  // divisor reciprocals of the direction cosines
-  double n0, n1, n2, n3, n4, n5;  // nodes of the current cell
-  double thr_abs, thr_trk;
+  double fx, fy, fz;  // the current cell's face planes ahead along x, y, z
+  double thr_abs;   // absorbed energy of the current cell visit
+  double thr_trk;   // the visit's track tally, set by a cutoff kill (visit_track)
   unsigned long long idx;
   Rng rng;
   uint32_t cell, group, ci, cj, ck, segs;
 };
 
-__device__ __forceinline__ void load_nodes(const MeshDev &m, Lane &L) {
-  L.n0 = m.x[L.ci]; L.n1 = m.x[L.ci + 1];
-  L.n2 = m.y[L.cj]; L.n3 = m.y[L.cj + 1];
-  L.n4 = m.z[L.ck]; L.n5 = m.z[L.ck + 1];
+// the node planes the photon moves toward along each axis: the upper one
+// for a positive direction cosine, else the lower one (the faces
+// get_distance_to_boundary measures to, cell.h:117-132)
+__device__ __forceinline__ void load_faces(const MeshDev &m, Lane &L) {
+  L.fx = m.x[L.ci + ((__double_as_longlong(L.dx) > 0) ? 1u : 0u)];
+  L.fy = m.y[L.cj + ((__double_as_longlong(L.dy) > 0) ? 1u : 0u)];
+  L.fz = m.z[L.ck + ((__double_as_longlong(L.dz) > 0) ? 1u : 0u)];
 }
 
 __device__ __forceinline__ void flush_tally(const CellsDev &c, const DeviceDiag *d, uint32_t cell,
                                             double a, double t, uint32_t &flags, int sa, int st) {
   unsigned long long lo, hi;
   TallyCell *tc = &c.tally[cell];
-  if (a != 0.0) {
+  // nonzero tests on the bit patterns (either sign of zero is zero)
+  if ((__double_as_longlong(a) << 1) != 0) {
     if (to_fixed128(a, sa, lo, hi)) atomic_add128(&tc->abs_lo, &tc->abs_hi, lo, hi);
     else flags |= (a == a) ? FLAG_TALLY_RANGE : FLAG_NAN;
   }
-  if (t != 0.0) {
+  if ((__double_as_longlong(t) << 1) != 0) {
     if (to_fixed128(t, st, lo, hi)) atomic_add128(&tc->trk_lo, &tc->trk_hi, lo, hi);
     else flags |= (t == t) ? FLAG_TALLY_RANGE : FLAG_NAN;
   }
@@ -165,6 +171,15 @@ __device__ __forceinline__ bool f64_positive(double x) { return __double_as_long
 // what one segment ends in (the event branches of transport_photon)
 enum SegEvent : int { SEG_KILLED = 0, SEG_SCATTER = 1, SEG_BOUNDARY = 2, SEG_CENSUS = 3 };
 
+// Track-length tally of the cell visit being flushed.  Upstream adds
+// absorbed/(sigma_a f) per segment (history_based_transport.h:75-77); sigma_a
+// f is constant within a visit, so it is formed once per visit from the
+// visit's absorbed sum (equal up to rounding).  A cutoff kill forms it
+// before the remaining weight is deposited (segment_advance).
+__device__ __forceinline__ double visit_track(const CellXS &xs, const Lane &L, int ev) {
+  return ev == SEG_KILLED ? L.thr_trk : L.thr_abs * xs.inv_saf;
+}
+
 // details of a segment the adjoint replay needs (unused elsewhere, so the
 // compiler drops them from the other kernels)
 struct SegInfo {
@@ -193,20 +208,24 @@ __device__ __forceinline__ int segment_advance(const CellXS &xs, Lane &L, uint32
   // -log(u) / sigma_eff with the integer, correctly rounded -log (bgs_fixmath.cuh)
   const double dist_to_scatter = scatters ? fix::neg_log_u53(L.rng.next_m53()) / xs.sig_eff : 1.0e100;
 #endif
-  // Cell::get_distance_to_boundary (cell.h:117-132); the comparisons are
-  // the upstream ones, evaluated on the integer keys
+  // Cell::get_distance_to_boundary (cell.h:117-132): the first face with
+  // the smallest (face - pos)/dir below 1e16, else 1e16 and face 0.  The
+  // comparisons are the upstream ones, evaluated on the integer keys.
   double dist_to_boundary = 1.0e16;
   long long k_boundary = f64_key(1.0e16);
   surface_cross = 0;
   const bool posx = f64_positive(L.dx), posy = f64_positive(L.dy), posz = f64_positive(L.dz);
+  const double ax = L.fx - L.px;
+  const double ay = L.fy - L.py;
+  const double az = L.fz - L.pz;
   {
-    double dist = seg_div((posx ? L.n1 : L.n0) - L.px, L.dx, L.rbx);
+    double dist = seg_div(ax, L.dx, L.rbx);
     long long k = f64_key(dist);
     if (k < k_boundary) { dist_to_boundary = dist; k_boundary = k; surface_cross = posx ? 1u : 0u; }
-    dist = seg_div((posy ? L.n3 : L.n2) - L.py, L.dy, L.rby);
+    dist = seg_div(ay, L.dy, L.rby);
     k = f64_key(dist);
     if (k < k_boundary) { dist_to_boundary = dist; k_boundary = k; surface_cross = posy ? 3u : 2u; }
-    dist = seg_div((posz ? L.n5 : L.n4) - L.pz, L.dz, L.rbz);
+    dist = seg_div(az, L.dz, L.rbz);
     k = f64_key(dist);
     if (k < k_boundary) { dist_to_boundary = dist; k_boundary = k; surface_cross = posz ? 5u : 4u; }
   }
@@ -222,7 +241,6 @@ __device__ __forceinline__ int segment_advance(const CellXS &xs, Lane &L, uint32
 
   const double absorbed_E = L.E * (1.0 - fix::exp_neg(-(xs.neg_saf * dist_to_event)));
   L.thr_abs += absorbed_E;
-  L.thr_trk += absorbed_E * xs.inv_saf;
   L.E = L.E - absorbed_E;
   L.px += L.dx * dist_to_event;  // Photon::move (photon.h:109-114)
   L.py += L.dy * dist_to_event;
@@ -242,6 +260,7 @@ __device__ __forceinline__ int segment_advance(const CellXS &xs, Lane &L, uint32
   if (k_e - k_thr <= 4 && k_thr - k_e <= 4) killed = L.E / L.E0 < kCutoff;
   if (killed || L.segs >= kMaxSegmentsPerHistory) {
     if (!killed) flags |= FLAG_SEGMENT_LIMIT;
+    L.thr_trk = L.thr_abs * xs.inv_saf;  // the visit's track tally, before the kill deposit
     L.thr_abs += L.E;
     return SEG_KILLED;
   }
@@ -264,11 +283,12 @@ __device__ __forceinline__ void scatter_update(const MeshDev &m, const CellsDev 
   L.dy = sin_theta * sp;
   L.dz = mu;
   direction_recips(L);
+  load_faces(m, L);
   // effective-scatter test and group resample (history_based_transport.h:97-98):
   // with sigma_s = 0 the test u > 0 always passes, and with one group the
   // walk always ends in group 0, so those draws only advance the counter
   bool resample;
-  if (xs.p_scat > 0.0) resample = L.rng.next() > xs.p_scat;
+  if (f64_positive(xs.p_scat)) resample = L.rng.next() > xs.p_scat;
   else { L.rng.skip(); resample = true; }
   if (resample) {
     if (m.n_groups > 1) L.group = sample_group(L.rng, c.group_v[L.cell], m.n_groups);
@@ -291,46 +311,51 @@ __device__ __forceinline__ int face_bc(const MeshDev &m, const Lane &L, uint32_t
   return interior ? ELEMENT : m.bc[surface_cross];
 }
 
-// ELEMENT crossing: the photon enters the neighbour (cell.h:110-112)
+// ELEMENT crossing: the photon enters the neighbour (cell.h:110-112); only
+// the crossed axis gets a new face ahead
 __device__ __forceinline__ void enter_neighbour(const MeshDev &m, Lane &L, uint32_t surface_cross) {
   switch (surface_cross) {
-    case 0: --L.ci; L.cell -= 1; break;
-    case 1: ++L.ci; L.cell += 1; break;
-    case 2: --L.cj; L.cell -= m.ngx; break;
-    case 3: ++L.cj; L.cell += m.ngx; break;
-    case 4: --L.ck; L.cell -= m.ngx * m.ngy; break;
-    default: ++L.ck; L.cell += m.ngx * m.ngy; break;
+    case 0: --L.ci; L.cell -= 1; L.fx = m.x[L.ci]; break;
+    case 1: ++L.ci; L.cell += 1; L.fx = m.x[L.ci + 1]; break;
+    case 2: --L.cj; L.cell -= m.ngx; L.fy = m.y[L.cj]; break;
+    case 3: ++L.cj; L.cell += m.ngx; L.fy = m.y[L.cj + 1]; break;
+    case 4: --L.ck; L.cell -= m.ngx * m.ngy; L.fz = m.z[L.ck]; break;
+    default: ++L.ck; L.cell += m.ngx * m.ngy; L.fz = m.z[L.ck + 1]; break;
   }
-  load_nodes(m, L);
 }
 
-// REFLECT: Photon::reflect (photon.h:151-155).  An integer divisor
-// reciprocal depends only on the magnitude; RN(1/-b) = -RN(1/b) exactly.
-__device__ __forceinline__ void reflect(Lane &L, uint32_t surface_cross) {
+// REFLECT: Photon::reflect (photon.h:151-155): the direction cosine flips
+// and the face ahead on that axis becomes the opposite plane of the cell.
+// An integer divisor reciprocal depends only on the magnitude; RN(1/-b) =
+// -RN(1/b) exactly.
+__device__ __forceinline__ void reflect(const MeshDev &m, Lane &L, uint32_t surface_cross) {
   if (surface_cross < 2) {
     L.dx = -L.dx;
 #if !BGS_INT_DIV
     L.rbx = -L.rbx;
 #endif
+    L.fx = m.x[L.ci + ((__double_as_longlong(L.dx) > 0) ? 1u : 0u)];
   } else if (surface_cross < 4) {
     L.dy = -L.dy;
 #if !BGS_INT_DIV
     L.rby = -L.rby;
 #endif
+    L.fy = m.y[L.cj + ((__double_as_longlong(L.dy) > 0) ? 1u : 0u)];
   } else {
     L.dz = -L.dz;
 #if !BGS_INT_DIV
     L.rbz = -L.rbz;
 #endif
+    L.fz = m.z[L.ck + ((__double_as_longlong(L.dz) > 0) ? 1u : 0u)];
   }
 }
 
-// cell coordinates and nodes from the global cell index
+// cell coordinates and the faces ahead from the global cell index
 __device__ __forceinline__ void locate(const MeshDev &m, Lane &L) {
   L.ci = L.cell % m.ngx;
   L.cj = (L.cell / m.ngx) % m.ngy;
   L.ck = L.cell / (m.ngx * m.ngy);
-  load_nodes(m, L);
+  load_faces(m, L);
 }
 
 }  // namespace bgs

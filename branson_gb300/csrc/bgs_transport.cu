@@ -62,9 +62,9 @@ __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
           L.rng.stream = b.stream[i]; L.rng.ctr = b.ctr[i]; L.rng.hi = seed_hi;
           L.segs = 0;
           if (kResume) {
-            L.thr_abs = es.thr_abs[i]; L.thr_trk = es.thr_trk[i];
+            L.thr_abs = es.thr_abs[i];
           } else {
-            L.thr_abs = 0.0; L.thr_trk = 0.0;
+            L.thr_abs = 0.0;
           }
           L.kill_thr = kCutoff * L.E0;
           direction_recips(L);
@@ -97,19 +97,18 @@ __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
     } else if (ev == SEG_BOUNDARY) {
       const int bc = face_bc(m, L, surface_cross);
       if (bc == ELEMENT) {
-        flush_tally(c, d, L.cell, L.thr_abs, L.thr_trk, flags, sa, st);
+        flush_tally(c, d, L.cell, L.thr_abs, visit_track(xs, L, ev), flags, sa, st);
         L.thr_abs = 0.0;
-        L.thr_trk = 0.0;
         enter_neighbour(m, L, surface_cross);
       } else if (bc == VACUUM || bc == SOURCE || bc == PROCESSOR) {
-        flush_tally(c, d, L.cell, L.thr_abs, L.thr_trk, flags, sa, st);
+        flush_tally(c, d, L.cell, L.thr_abs, visit_track(xs, L, ev), flags, sa, st);
         store_end(b, L, bc == PROCESSOR ? PASS : EXIT);
         active = false;
       } else {
-        reflect(L, surface_cross);
+        reflect(m, L, surface_cross);
       }
     } else {  // SEG_CENSUS
-      flush_tally(c, d, L.cell, L.thr_abs, L.thr_trk, flags, sa, st);
+      flush_tally(c, d, L.cell, L.thr_abs, visit_track(xs, L, ev), flags, sa, st);
       store_end(b, L, CENSUS);
       active = false;
     }
