@@ -81,6 +81,8 @@ class Deck:
     n_omp_threads: int = 1
     batch_size: int = 100000000
     use_gpu_transporter: bool = False
+    write_silo: bool = False     # field output every output_frequency steps (input.h:143, :169-173)
+    output_frequency: int = 1
     x_divisions: List[Division] = dataclasses.field(default_factory=list)
     y_divisions: List[Division] = dataclasses.field(default_factory=list)
     z_divisions: List[Division] = dataclasses.field(default_factory=list)
@@ -163,7 +165,8 @@ class Deck:
                   f"    <particle_algorithm>{algo}</particle_algorithm>",
                   f"    <n_omp_threads>{int(self.n_omp_threads)}</n_omp_threads>",
                   f"    <batch_size>{int(self.batch_size)}</batch_size>",
-                  "    <output_frequency>1</output_frequency>",
+                  f"    <output_frequency>{int(self.output_frequency)}</output_frequency>",
+                  f"    <write_silo>{'TRUE' if self.write_silo else 'FALSE'}</write_silo>",
                   "  </common>",
                   "  <debug_options><print_verbose>FALSE</print_verbose>"
                   "<print_mesh_info>FALSE</print_mesh_info></debug_options>",
@@ -244,6 +247,9 @@ def parse_xml(text: str, n_groups: int = 1) -> Deck:
     deck.photons = int(_text(common, "photons") or 0)
     deck.seed = int(_text(common, "seed") or 0) & 0xFFFFFFFF
     deck.use_gpu_transporter = _text(common, "use_gpu_transporter") == "TRUE"
+    deck.write_silo = _text(common, "write_silo") == "TRUE"
+    t = _text(common, "output_frequency")
+    deck.output_frequency = int(t) if t else 0
     deck.algorithm = EVENT if _text(common, "particle_algorithm") == "EVENT" else HISTORY
     t = _text(common, "n_omp_threads")
     deck.n_omp_threads = int(t) if t else 1
