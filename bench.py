@@ -161,14 +161,17 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def cpu_port_rate(dk_gpu, photons: float, threads: int, steps: int = 1):
-    """Oracle (C port of the upstream history loop) on the host cores."""
+def cpu_port_rate(dk_gpu, photons: float, threads: int, steps: int = 1, warmup: int = 0):
+    """Oracle (C port of the upstream history loop) on the host cores, timed
+    over `steps` steps after `warmup` untimed ones (the GPU arm's steps)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import copy
     import oracle as O
     dk = copy.deepcopy(dk_gpu)
     dk.photons = int(photons)
     orc = O.Oracle(dk, n_threads=threads)
+    for _ in range(warmup):
+        orc.step()
     hist = 0
     secs = 0.0
     segs = 0
@@ -245,7 +248,7 @@ def run_ours(args, rank, world, local):
     if not args.no_tune:
         from branson_gb300.tune import tune
         res = tune(imc, repeats=2)
-        tuning = {"schedule": res.best.label(), "transport_ms": res.best_ms,
+        tuning = {"schedule": res.best.label(), "transport_ms": res.best_ms, "algorithm": imc.algorithm,
                   "candidates": {c.label(): ms for c, ms in res.timings}}
 
     for _ in range(args.warmup):
@@ -302,10 +305,10 @@ def run_ours(args, rank, world, local):
     cpu = None
     if not args.no_cpu_baseline and rank == 0 and world == 1:
         threads = os.cpu_count() or 1
-        h, s, sg = cpu_port_rate(dk, args.cpu_photons, threads)
+        h, s, sg = cpu_port_rate(dk, args.cpu_photons, threads, steps=1, warmup=args.warmup)
         cpu = {"value": h / s, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"1 step of the same deck at {int(args.cpu_photons)} photons ({h} histories), "
-                         f"transport time"}
+               "sample": f"step {args.warmup + 1} (after {args.warmup} untimed, as the GPU arm) of the same "
+                         f"deck at {int(args.cpu_photons)} photons ({h} histories), transport time"}
     imc.close()
     adjoint = None
     if not args.no_adjoint and rank == 0 and world == 1:
@@ -358,6 +361,40 @@ def e2e_dropin(imc, dk, args):
             "d2h_bytes_per_step": int(out_bytes), "call": "bgs_replicated_transport", "steps": k}
 
 
+def batch_adjoint_timing(b):
+    """Adjoint of every problem's next step: the forwards (per problem), then
+    dL/dsigma_a for all problems from one replay launch, against the same
+    backwards called problem by problem (same tapes and weights, equal
+    results)."""
+    import numpy as np
+    from branson_gb300.adjoint import batch_backward, batch_forward
+    rng = np.random.default_rng(777)
+    t0 = time.perf_counter()
+    _, tapes = batch_forward(b)
+    fwd = time.perf_counter() - t0
+    ws = [rng.uniform(0.0, 1.0, p.n_cells) for p in b.problems]
+    batch_backward(b, tapes, ws)  # warm-up (scratch allocation)
+    t0 = time.perf_counter()
+    grads = batch_backward(b, tapes, ws)
+    bwd = time.perf_counter() - t0
+    replay_ms = tapes[0].info()["replay_ms"]
+    t0 = time.perf_counter()
+    same = True
+    for p, t, w, g in zip(b.problems, tapes, ws, grads):
+        own = np.empty(p.n_cells)
+        if b.lib.bgs_adjoint_backward(p.ctx, t.handle, w.ctypes.data, own.ctypes.data) != 0:
+            raise RuntimeError("bgs_adjoint_backward failed")
+        same &= bool(np.array_equal(own, g))
+    seq = time.perf_counter() - t0
+    hist = sum(t.info()["n_histories"] for t in tapes)
+    for t in tapes:
+        t.close()
+    return {"histories": int(hist), "forward_s": fwd, "batched_backward_s": bwd,
+            "batched_replay_kernel_ms": replay_ms, "sequential_backward_s": seq,
+            "batched_backward_over_sequential": seq / bwd, "backward_over_forward": bwd / fwd,
+            "equal_to_per_problem": same}
+
+
 def batch_bench(args, dev, steps: int = 2):
     """Batching workload: 256 independent problems (master seed 777), cubic
     meshes of side U{8..64} on [0,1]^3, photons lognormal (median 1e5)
@@ -397,6 +434,7 @@ def batch_bench(args, dev, steps: int = 2):
         for p in probs:
             p.close()
     bat = {"s": [], "hist": [], "seg": [], "transport_ms": []}
+    adj = None
     with BatchIMC(decks, device=dev) as b:
         launches0 = b.last_transport_ms()[1]
         for _ in range(steps):
@@ -407,6 +445,8 @@ def batch_bench(args, dev, steps: int = 2):
             bat["seg"].append(sum(r.n_segments for r in reps))
             bat["transport_ms"].append(b.last_transport_ms()[0])
         launches = b.last_transport_ms()[1] - launches0
+        if not args.no_adjoint:
+            adj = batch_adjoint_timing(b)
     assert seq["hist"] == bat["hist"] and seq["seg"] == bat["seg"], "batched and sequential runs disagree"
     rate_s = sum(seq["hist"]) / sum(seq["s"])
     rate_b = sum(bat["hist"]) / sum(bat["s"])
@@ -419,6 +459,7 @@ def batch_bench(args, dev, steps: int = 2):
             "sequential_transport_kernel_ms_sum": seq["transport_ms"],
             "batched_segments_per_s": sum(bat["seg"]) / sum(bat["s"]),
             "kernel_launches_per_batched_step": launches // steps,
+            "adjoint": adj,
             "timing": "host wall clock around each whole step (sync), same problems and results in both arms"}
 
 

@@ -116,6 +116,9 @@ SIGNATURES = (
     ("bgs_batch_synchronize", C.c_int, [C.c_void_p]),
     ("bgs_batch_set_option", C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     ("bgs_batch_last_transport_ms", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_uint64)]),
+    ("bgs_batch_adjoint_forward", C.c_int,
+     [C.c_void_p, C.POINTER(StepParams), C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
+    ("bgs_batch_adjoint_backward", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_void_p, C.c_void_p]),
     ("bgs_set_option", C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     ("bgs_last_transport_ms", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_uint32)]),
     ("bgs_kernel_launch_count", C.c_uint64, [C.c_void_p]),

@@ -122,3 +122,62 @@ def absorbed_energy(step: AdjointStep, sigma_a, counts: Optional[np.ndarray] = N
             return torch.from_numpy(g)
 
     return _AbsorbedEnergy.apply(sigma_a)
+
+
+def batch_forward(batch, sigma_a=None, counts=None, tapes=None):
+    """bgs_batch_adjoint_forward: the adjoint forward of every problem of a
+    BatchIMC at its current step.  sigma_a / counts: None or one entry per
+    problem (each None or an array).  Returns (abs_E list, tape list)."""
+    probs = batch.problems
+    n = len(probs)
+    params = (_lib.StepParams * n)()
+    for i, p in enumerate(probs):
+        nd = p.next_dt()
+        params[i] = _lib.StepParams(p.step_no, _lib.HISTORY, p.dt, nd if nd > 0.0 else p.dt)
+    keep = []
+
+    def ptr_array(items, dtype):
+        if items is None:
+            return None
+        arr = (C.c_void_p * n)()
+        for i, a in enumerate(items):
+            if a is not None:
+                a = np.ascontiguousarray(a, dtype=dtype)
+                keep.append(a)
+                arr[i] = a.ctypes.data
+        return arr
+
+    sig = ptr_array(sigma_a, np.float64)
+    cnt = ptr_array(counts, np.uint32)
+    abs_out = [np.empty(p.n_cells) for p in probs]
+    abs_ptrs = (C.c_void_p * n)(*[a.ctypes.data for a in abs_out])
+    handles = (C.c_void_p * n)()
+    if tapes is not None:
+        for i, t in enumerate(tapes):
+            handles[i] = t.handle.value if t is not None and t.handle else None
+    batch._check(batch.lib.bgs_batch_adjoint_forward(batch.handle, params, sig, cnt, abs_ptrs, handles),
+                 "bgs_batch_adjoint_forward")
+    out_tapes = []
+    for i, p in enumerate(probs):
+        h = C.c_void_p(handles[i])
+        if tapes is not None and tapes[i] is not None:
+            tapes[i].handle = h
+            out_tapes.append(tapes[i])
+        else:
+            out_tapes.append(Tape(batch.lib, h, p.n_cells))
+    return abs_out, out_tapes
+
+
+def batch_backward(batch, tapes, grads):
+    """bgs_batch_adjoint_backward: every problem's dL/dsigma_a from its tape
+    and dL/dE_abs, in one replay launch."""
+    probs = batch.problems
+    n = len(probs)
+    w = [np.ascontiguousarray(g, dtype=np.float64) for g in grads]
+    out = [np.empty(p.n_cells) for p in probs]
+    handles = (C.c_void_p * n)(*[t.handle.value for t in tapes])
+    w_ptrs = (C.c_void_p * n)(*[a.ctypes.data for a in w])
+    o_ptrs = (C.c_void_p * n)(*[a.ctypes.data for a in out])
+    batch._check(batch.lib.bgs_batch_adjoint_backward(batch.handle, handles, w_ptrs, o_ptrs),
+                 "bgs_batch_adjoint_backward")
+    return out

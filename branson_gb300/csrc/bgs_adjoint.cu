@@ -18,6 +18,9 @@
 // depend on sigma_a, the group choice does not enter L, and the E/E0 < 0.01
 // cutoff is a threshold that the estimator does not differentiate.
 //
+// A launch replays the saved histories of one or many problems (a batched
+// backward): work items are all problems' histories, concatenated.
+//
 // future = G - running prefix: per cell visit the terms add up to
 // G * A_v - B_v with A_v, B_v accumulated during the visit, so one replay
 // logs (cell, A_v, B_v) per visit in a per-thread slot and flushes G A_v -
@@ -38,30 +41,36 @@ constexpr int kAdjThreads = 128;
 #endif
 constexpr uint8_t kEmission = 2;  // Photon source type of emission photons
 
-__device__ __forceinline__ void flush_grad(const AdjointDev &a, uint32_t cell, double v, uint32_t &flags) {
-  if (v == 0.0) return;
-  if (!(fabs(v) <= a.visit_bound)) {
+__device__ __forceinline__ void flush_grad(const AdjProblem &P, uint32_t cell, double v, uint32_t &flags) {
+  if ((__double_as_longlong(v) << 1) == 0) return;
+  if (!(fabs(v) <= P.visit_bound)) {
     flags |= (v == v) ? FLAG_TALLY_RANGE : FLAG_NAN;
     return;
   }
   unsigned long long lo, hi;
-  to_fixed128_signed(v, a.scale, lo, hi);
-  atomic_add128(&a.grad[2 * (size_t)cell], &a.grad[2 * (size_t)cell + 1], lo, hi);
+  to_fixed128_signed(v, P.scale, lo, hi);
+  atomic_add128(&P.grad[2 * (size_t)cell], &P.grad[2 * (size_t)cell + 1], lo, hi);
 }
 
+// Work items are the saved histories of all problems of the launch
+// (item_off: exclusive prefix sum); a lane finds its problem at pickup.
 // kPass 0: every history, logged; 1: totals of the listed long histories;
 // 2: gradients of the listed long histories with their totals known.
 template <int kPass>
 __global__ void __launch_bounds__(kAdjThreads, BGS_ADJ_MIN_BLOCKS)
-    k_adjoint_replay(MeshDev m, CellsDev c, Bank t, AdjointDev a, unsigned long long seed_hi) {
-  const unsigned long long n = kPass == 0 ? a.n : (unsigned long long)*a.n_long;
+    k_adjoint_replay(const AdjProblem *__restrict__ probs, uint32_t n_probs,
+                     const unsigned long long *__restrict__ item_off, AdjShared a) {
+  const unsigned long long n = kPass == 0 ? item_off[n_probs] : (unsigned long long)*a.n_long;
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lanemask_lt = (1u << lane) - 1u;
   const size_t log_base = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) * a.log_len;
   uint32_t flags = 0;
   Lane L;
   bool active = false, done = false, overflow = false;
-  unsigned long long item = 0;
+  unsigned long long item = 0, gitem = 0;
+  uint32_t p = 0;
+  const CellXS *xs_p = nullptr;
+  const AdjCell *ac_p = nullptr;
   double prefix = 0.0, vis_a = 0.0, vis_b = 0.0, G = 0.0;
   uint32_t n_log = 0;
 
@@ -76,33 +85,39 @@ __global__ void __launch_bounds__(kAdjThreads, BGS_ADJ_MIN_BLOCKS)
         const unsigned long long w = base + __popc(need & lanemask_lt);
         if (w < n) {
           item = w;
-          const unsigned long long i = kPass == 0 ? w : (unsigned long long)a.long_list[w];
+          gitem = kPass == 0 ? w : a.long_list[w];
+          p = problem_of(item_off, n_probs, gitem);
+          const AdjProblem &P = probs[p];
+          const Bank &t = P.t;
+          const unsigned long long i = gitem - item_off[p];
           L.idx = i;
           L.px = t.px[i]; L.py = t.py[i]; L.pz = t.pz[i];
           L.dx = t.dx[i]; L.dy = t.dy[i]; L.dz = t.dz[i];
           L.E = t.E[i]; L.E0 = t.E0[i]; L.life = t.life[i];
           L.cell = t.cell[i]; L.group = t.group[i];
-          L.rng.stream = t.stream[i]; L.rng.ctr = t.ctr[i]; L.rng.hi = seed_hi;
+          L.rng.stream = t.stream[i]; L.rng.ctr = t.ctr[i]; L.rng.hi = P.seed_hi;
           L.segs = 0;
           L.thr_abs = 0.0;
           L.kill_thr = kCutoff * L.E0;
           direction_recips(L);
+          xs_p = P.xs;
+          ac_p = P.cell;
           prefix = 0.0; vis_a = 0.0; vis_b = 0.0;
           n_log = 0;
           overflow = false;
           G = kPass == 2 ? a.long_G[w] : 0.0;
-          if (L.cell < m.n_cells) {
-            locate(m, L);
+          if (L.cell < P.m.n_cells) {
+            locate(P.m, L);
             active = true;
             if (t.stype[i] == kEmission) {  // source-weight term, a visit of its own
-              const double s = a.src[L.cell];
+              const double s = P.src[L.cell];
               if (kPass == 0) {
                 a.log_a[log_base] = s;
                 a.log_b[log_base] = 0.0;
                 a.log_cell[log_base] = L.cell;
                 n_log = 1;
               } else if (kPass == 2) {
-                flush_grad(a, L.cell, G * s - 0.0, flags);
+                flush_grad(P, L.cell, G * s - 0.0, flags);
               }
             }
           } else {
@@ -117,8 +132,8 @@ __global__ void __launch_bounds__(kAdjThreads, BGS_ADJ_MIN_BLOCKS)
     if (!active) continue;
 
     // ---- one segment, as in the forward transport
-    const CellXS xs = c.xs[L.cell];
-    const AdjCell ac = a.cell[L.cell];
+    const CellXS xs = xs_p[L.cell];
+    const AdjCell ac = ac_p[L.cell];
     uint32_t surface_cross;
     SegInfo info;
     const int ev = segment_advance(xs, L, surface_cross, flags, &info);
@@ -137,8 +152,11 @@ __global__ void __launch_bounds__(kAdjThreads, BGS_ADJ_MIN_BLOCKS)
     if (ev == SEG_KILLED || ev == SEG_CENSUS) {
       end = true;
     } else if (ev == SEG_SCATTER) {
-      scatter_update(m, c, xs, L);
+      CellsDev c{};
+      c.group_v = const_cast<double *>(probs[p].group_v);
+      scatter_update(probs[p].m, c, xs, L);
     } else {
+      const MeshDev &m = probs[p].m;
       const int bc = face_bc(m, L, surface_cross);
       if (bc == ELEMENT) leave = true;
       else if (bc == VACUUM || bc == SOURCE || bc == PROCESSOR) end = true;
@@ -155,22 +173,23 @@ __global__ void __launch_bounds__(kAdjThreads, BGS_ADJ_MIN_BLOCKS)
           overflow = true;
         }
       } else if (kPass == 2) {
-        flush_grad(a, L.cell, G * vis_a - vis_b, flags);
+        flush_grad(probs[p], L.cell, G * vis_a - vis_b, flags);
       }
       vis_a = 0.0;
       vis_b = 0.0;
-      if (leave) enter_neighbour(m, L, surface_cross);
+      if (leave) enter_neighbour(probs[p].m, L, surface_cross);
     }
     if (end) {
       active = false;
       if (kPass == 0) {
         if (overflow) {
           const unsigned int q = atomicAdd(a.n_long, 1u);
-          a.long_list[q] = (uint32_t)L.idx;
+          a.long_list[q] = gitem;
         } else {
           G = prefix;
+          const AdjProblem &P = probs[p];
           for (uint32_t k = 0; k < n_log; ++k)
-            flush_grad(a, a.log_cell[log_base + k], G * a.log_a[log_base + k] - a.log_b[log_base + k], flags);
+            flush_grad(P, a.log_cell[log_base + k], G * a.log_a[log_base + k] - a.log_b[log_base + k], flags);
         }
       } else if (kPass == 1) {
         a.long_G[item] = prefix;
@@ -237,15 +256,14 @@ void launch_adjoint_set_w(uint32_t n_cells, AdjCell *adj, const double *w, cudaS
 }
 
 // the three passes; passes 1 and 2 find an empty list in the common case
-void launch_adjoint_replay(const MeshDev &m, const CellsDev &c, const Bank &tape, const AdjointDev &a,
-                           uint32_t seed, const TransportLaunch &shape, cudaStream_t s) {
-  const unsigned long long seed_hi = (unsigned long long)seed << 32;
+void launch_adjoint_replay(const AdjProblem *probs, uint32_t n, const unsigned long long *item_off,
+                           const AdjShared &a, const TransportLaunch &shape, cudaStream_t s) {
   cudaMemsetAsync(a.work, 0, sizeof(unsigned long long), s);
-  k_adjoint_replay<0><<<shape.blocks, shape.threads, 0, s>>>(m, c, tape, a, seed_hi);
+  k_adjoint_replay<0><<<shape.blocks, shape.threads, 0, s>>>(probs, n, item_off, a);
   cudaMemsetAsync(a.work, 0, sizeof(unsigned long long), s);
-  k_adjoint_replay<1><<<shape.blocks, shape.threads, 0, s>>>(m, c, tape, a, seed_hi);
+  k_adjoint_replay<1><<<shape.blocks, shape.threads, 0, s>>>(probs, n, item_off, a);
   cudaMemsetAsync(a.work, 0, sizeof(unsigned long long), s);
-  k_adjoint_replay<2><<<shape.blocks, shape.threads, 0, s>>>(m, c, tape, a, seed_hi);
+  k_adjoint_replay<2><<<shape.blocks, shape.threads, 0, s>>>(probs, n, item_off, a);
 }
 
 void launch_adjoint_grad_to_double(uint32_t n_cells, const unsigned long long *grad, int scale, double *out,

@@ -25,9 +25,7 @@ struct bgs_adjoint_tape {
   double *src = nullptr;
   double *w = nullptr, *grad_out = nullptr;
   unsigned long long *grad = nullptr;
-  uint32_t *long_list = nullptr;
-  double *long_G = nullptr;
-  unsigned long long *scalars = nullptr;  // [0] coefficient max bits, [1] n_long, [2] flags
+  unsigned long long *scalars = nullptr;  // [0] coefficient max bits
   std::vector<uint32_t> counts;           // emission | boundary source | initial census, per cell
   double max_E = 0.0, max_life = 0.0, coef_max = 0.0;
   unsigned long long n_segments = 0;
@@ -57,7 +55,6 @@ int alloc_tape(bgs_context *ctx, bgs_adjoint_tape *t, unsigned long long cap, ui
       (rc = dev_alloc(ctx, L, &b.life, cap)) || (rc = dev_alloc(ctx, L, &b.cell, cap)) ||
       (rc = dev_alloc(ctx, L, &b.group, cap)) || (rc = dev_alloc(ctx, L, &b.stype, cap)) ||
       (rc = dev_alloc(ctx, L, &b.stream, cap)) || (rc = dev_alloc(ctx, L, &b.ctr, cap)) ||
-      (rc = dev_alloc(ctx, L, &t->long_list, cap)) || (rc = dev_alloc(ctx, L, &t->long_G, cap)) ||
       (rc = dev_alloc(ctx, L, &t->xs, n_cells)) || (rc = dev_alloc(ctx, L, &t->group_v, n_cells)) ||
       (rc = dev_alloc(ctx, L, &t->adj, n_cells)) || (rc = dev_alloc(ctx, L, &t->src, n_cells)) ||
       (rc = dev_alloc(ctx, L, &t->w, n_cells)) || (rc = dev_alloc(ctx, L, &t->grad_out, n_cells)) ||
@@ -86,15 +83,32 @@ int copy_bank(bgs_context *ctx, const Bank &from, const Bank &to, unsigned long 
   return BGS_OK;
 }
 
-int ensure_replay_scratch(bgs_context *ctx) {
-  if (ctx->adj_log_a) return BGS_OK;
-  ctx->adj_shape = adjoint_launch_shape(ctx->n_sm);
-  const size_t slots = (size_t)ctx->adj_shape.blocks * ctx->adj_shape.threads * ctx->adj_log_len;
-  int rc;
+// Replay scratch of a context, grown to `items` saved histories and `n`
+// problems: per-thread visit logs, the long-history list, counters, and the
+// problem table with its item offsets (device, and pinned host staging).
+int ensure_replay_scratch(bgs_context *ctx, unsigned long long items, uint32_t n) {
   auto &L = ctx->adj_allocs;
-  if ((rc = dev_alloc(ctx, L, &ctx->adj_log_a, slots)) || (rc = dev_alloc(ctx, L, &ctx->adj_log_b, slots)) ||
-      (rc = dev_alloc(ctx, L, &ctx->adj_log_cell, slots)) || (rc = dev_alloc(ctx, L, &ctx->adj_work, 1)))
-    return rc;
+  int rc;
+  if (!ctx->adj_log_a) {
+    ctx->adj_shape = adjoint_launch_shape(ctx->n_sm);
+    const size_t slots = (size_t)ctx->adj_shape.blocks * ctx->adj_shape.threads * ctx->adj_log_len;
+    if ((rc = dev_alloc(ctx, L, &ctx->adj_log_a, slots)) || (rc = dev_alloc(ctx, L, &ctx->adj_log_b, slots)) ||
+        (rc = dev_alloc(ctx, L, &ctx->adj_log_cell, slots)) || (rc = dev_alloc(ctx, L, &ctx->adj_work, 4)))
+      return rc;
+  }
+  if (items > ctx->adj_items_cap) {
+    const unsigned long long cap = items > 1024 ? items : 1024;
+    if ((rc = dev_alloc(ctx, L, &ctx->adj_long_list, cap)) || (rc = dev_alloc(ctx, L, &ctx->adj_long_G, cap)))
+      return rc;
+    ctx->adj_items_cap = cap;
+  }
+  if (n > ctx->adj_probs_cap) {
+    if ((rc = dev_alloc(ctx, L, &ctx->adj_probs, n)) || (rc = dev_alloc(ctx, L, &ctx->adj_item_off, (size_t)n + 1)))
+      return rc;
+    ctx->h_adj_probs.resize(n);
+    ctx->h_adj_item_off.resize((size_t)n + 1);
+    ctx->adj_probs_cap = n;
+  }
   return BGS_OK;
 }
 
@@ -102,6 +116,118 @@ double bits_to_double(unsigned long long b) {
   double v;
   std::memcpy(&v, &b, sizeof(v));
   return v;
+}
+
+// Backward of n saved forwards in one replay launch: tapes[i] was made on
+// ctxs[i]; owner supplies the stream, the events and the scratch.
+int replay_backward(bgs_context *owner, bgs_context *const *ctxs, bgs_adjoint_tape *const *tapes, uint32_t n,
+                    const double *const *w, double *const *out) {
+  bgs_context *ctx = owner;
+  unsigned long long items = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    const bgs_adjoint_tape *t = tapes[i];
+    const bgs_context *c = ctxs[i];
+    if (!t || !c || !w[i] || !out[i]) return fail(ctx, BGS_ERR_INVALID, "problem %u: null tape, context or array", i);
+    if (!t->valid) return fail(ctx, BGS_ERR_STATE, "problem %u: the tape holds no completed forward", i);
+    if (t->device != ctx->device || c->device != ctx->device)
+      return fail(ctx, BGS_ERR_INVALID, "problem %u: the tape belongs to device %d", i, t->device);
+    if (!c->has_mesh || t->mesh_generation != c->mesh_generation || t->n_cells != c->mesh.n_cells)
+      return fail(ctx, BGS_ERR_STATE, "problem %u: the mesh changed since the forward", i);
+    items += t->n;
+  }
+  if (items >= 0xffffffffULL * 4096ULL) return fail(ctx, BGS_ERR_CAPACITY, "too many saved histories");
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  if ((rc = ensure_replay_scratch(ctx, items, n))) return rc;
+  cudaStream_t s = ctx->stream;
+  std::vector<int> scales(n);
+  std::vector<double> bounds(n);
+  unsigned long long off = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    bgs_adjoint_tape *t = tapes[i];
+    const bgs_context *c = ctxs[i];
+    const uint32_t nc = t->n_cells;
+    double wmax = 0.0;
+    for (uint32_t g = 0; g < nc; ++g) {
+      if (!std::isfinite(w[i][g])) return fail(ctx, BGS_ERR_INVALID, "problem %u: grad_abs_E[%u] is not finite", i, g);
+      wmax = std::fmax(wmax, std::fabs(w[i][g]));
+    }
+    // Range of one visit's contribution G*A - B: |G| <= wmax * E_start, and
+    // per unit weight the coefficients sum to at most 3 * flight length plus
+    // the per-collision and source coefficients; 2^12 of headroom, and every
+    // visit is checked against the bound, so the sum over all visits (at most
+    // segments + histories of them) stays inside 2^118.
+    const double visit_bound = wmax * t->max_E * (3.0 * t->max_life + 8.0 * t->coef_max) * 4096.0;
+    const double n_terms = (double)(t->n_segments + t->n + 1);
+    int scale = 0;
+    if (visit_bound > 0.0) {
+      int e;
+      std::frexp(visit_bound * n_terms, &e);
+      scale = 118 - e;
+    }
+    scales[i] = scale;
+    bounds[i] = visit_bound;
+    BGS_CUDA(ctx, cudaMemcpyAsync(t->w, w[i], nc * sizeof(double), cudaMemcpyHostToDevice, s));
+    launch_adjoint_set_w(nc, t->adj, t->w, s);
+    BGS_LAUNCHED(ctx, 1);
+    BGS_CUDA(ctx, cudaMemsetAsync(t->grad, 0, 2 * (size_t)nc * sizeof(unsigned long long), s));
+    AdjProblem P{};
+    P.m = c->mesh;
+    P.xs = t->xs;
+    P.group_v = t->group_v;
+    P.t = t->bank;
+    P.cell = t->adj;
+    P.src = t->src;
+    P.grad = t->grad;
+    P.seed_hi = (unsigned long long)t->seed << 32;
+    P.visit_bound = visit_bound;
+    P.scale = scale;
+    ctx->h_adj_probs[i] = P;
+    ctx->h_adj_item_off[i] = off;
+    off += t->n;
+  }
+  ctx->h_adj_item_off[n] = off;
+  // (pageable staging: the copies complete before the calls return)
+  BGS_CUDA(ctx, cudaMemcpyAsync(ctx->adj_probs, ctx->h_adj_probs.data(), n * sizeof(AdjProblem),
+                                cudaMemcpyHostToDevice, s));
+  BGS_CUDA(ctx, cudaMemcpyAsync(ctx->adj_item_off, ctx->h_adj_item_off.data(), ((size_t)n + 1) * sizeof(unsigned long long),
+                                cudaMemcpyHostToDevice, s));
+  BGS_CUDA(ctx, cudaMemsetAsync(ctx->adj_work + 1, 0, 2 * sizeof(unsigned long long), s));
+  AdjShared a{};
+  a.log_a = ctx->adj_log_a;
+  a.log_b = ctx->adj_log_b;
+  a.log_cell = ctx->adj_log_cell;
+  a.log_len = ctx->adj_log_len;
+  a.long_list = ctx->adj_long_list;
+  a.long_G = ctx->adj_long_G;
+  a.n_long = reinterpret_cast<unsigned int *>(ctx->adj_work + 1);
+  a.work = ctx->adj_work;
+  a.flags = reinterpret_cast<uint32_t *>(ctx->adj_work + 2);
+  BGS_CUDA(ctx, cudaEventRecord(ctx->ev0, s));
+  launch_adjoint_replay(ctx->adj_probs, n, ctx->adj_item_off, a, ctx->adj_shape, s);
+  BGS_LAUNCHED(ctx, 3);
+  BGS_CUDA(ctx, cudaEventRecord(ctx->ev1, s));
+  for (uint32_t i = 0; i < n; ++i) {
+    bgs_adjoint_tape *t = tapes[i];
+    launch_adjoint_grad_to_double(t->n_cells, t->grad, scales[i], t->grad_out, s);
+    BGS_LAUNCHED(ctx, 1);
+    BGS_CUDA(ctx, cudaMemcpyAsync(out[i], t->grad_out, t->n_cells * sizeof(double), cudaMemcpyDeviceToHost, s));
+  }
+  unsigned long long sc[2];
+  BGS_CUDA(ctx, cudaMemcpyAsync(sc, ctx->adj_work + 1, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+  BGS_CUDA(ctx, cudaStreamSynchronize(s));
+  float ms = 0.0f;
+  BGS_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  for (uint32_t i = 0; i < n; ++i) {
+    bgs_adjoint_tape *t = tapes[i];
+    t->info.n_long = (uint32_t)sc[0];
+    t->info.grad_scale = scales[i];
+    t->info.device_flags = (uint32_t)sc[1];
+    t->info.visit_bound = bounds[i];
+    t->info.replay_ms = ms;
+  }
+  if (sc[1]) return check_flags(ctx, (uint32_t)sc[1]);
+  return BGS_OK;
 }
 
 }  // namespace
@@ -223,79 +349,35 @@ int bgs_adjoint_forward(bgs_context *ctx, const bgs_step_params *p, const double
 
 int bgs_adjoint_backward(bgs_context *ctx, bgs_adjoint_tape *t, const double *grad_abs_E, double *grad_sigma_a) {
   if (!ctx || !t || !grad_abs_E || !grad_sigma_a) return BGS_ERR_INVALID;
-  if (!t->valid) return fail(ctx, BGS_ERR_STATE, "the tape holds no completed forward");
-  if (t->device != ctx->device) return fail(ctx, BGS_ERR_INVALID, "the tape belongs to device %d", t->device);
-  if (!ctx->has_mesh || t->mesh_generation != ctx->mesh_generation || t->n_cells != ctx->mesh.n_cells)
-    return fail(ctx, BGS_ERR_STATE, "the mesh changed since the forward");
-  int rc = set_device(ctx);
+  bgs_context *ctxs[1] = {ctx};
+  bgs_adjoint_tape *tapes[1] = {t};
+  const double *w[1] = {grad_abs_E};
+  double *out[1] = {grad_sigma_a};
+  return replay_backward(ctx, ctxs, tapes, 1, w, out);
+}
+
+int bgs_batch_adjoint_forward(bgs_batch *b, const bgs_step_params *params, const double *const *sigma_a,
+                              const uint32_t *const *counts, double *const *abs_E, bgs_adjoint_tape **tapes) {
+  if (!b || !params || !abs_E || !tapes) return BGS_ERR_INVALID;
+  int rc = bgs_batch_synchronize(b);
   if (rc) return rc;
-  if ((rc = ensure_replay_scratch(ctx))) return rc;
-  const uint32_t nc = t->n_cells;
-  cudaStream_t s = ctx->stream;
-
-  double wmax = 0.0;
-  for (uint32_t g = 0; g < nc; ++g) {
-    if (!std::isfinite(grad_abs_E[g]))
-      return fail(ctx, BGS_ERR_INVALID, "grad_abs_E[%u] is not finite", g);
-    wmax = std::fmax(wmax, std::fabs(grad_abs_E[g]));
+  const std::vector<bgs_context *> &ctx = batch_contexts(b);
+  for (uint32_t i = 0; i < (uint32_t)ctx.size(); ++i) {
+    rc = bgs_adjoint_forward(ctx[i], &params[i], sigma_a ? sigma_a[i] : nullptr, counts ? counts[i] : nullptr,
+                             abs_E[i], &tapes[i]);
+    if (rc) return batch_fail(b, rc, "problem " + std::to_string(i) + ": " + ctx[i]->err);
   }
-  // Range of one visit's contribution G*A - B: |G| <= wmax * E_start, and
-  // per unit weight the coefficients sum to at most 3 * flight length plus
-  // the per-collision and source coefficients; 2^12 of headroom, and every
-  // visit is checked against the bound, so the sum over all visits (at most
-  // segments + histories of them) stays inside 2^118.
-  const double visit_bound = wmax * t->max_E * (3.0 * t->max_life + 8.0 * t->coef_max) * 4096.0;
-  const double n_terms = (double)(t->n_segments + t->n + 1);
-  int scale = 0;
-  if (visit_bound > 0.0) {
-    int e;
-    std::frexp(visit_bound * n_terms, &e);
-    scale = 118 - e;
-  }
+  return BGS_OK;
+}
 
-  BGS_CUDA(ctx, cudaMemcpyAsync(t->w, grad_abs_E, nc * sizeof(double), cudaMemcpyHostToDevice, s));
-  launch_adjoint_set_w(nc, t->adj, t->w, s);
-  BGS_LAUNCHED(ctx, 1);
-  BGS_CUDA(ctx, cudaMemsetAsync(t->grad, 0, 2 * (size_t)nc * sizeof(unsigned long long), s));
-  BGS_CUDA(ctx, cudaMemsetAsync(t->scalars + 1, 0, 2 * sizeof(unsigned long long), s));
-
-  AdjointDev a{};
-  a.cell = t->adj;
-  a.src = t->src;
-  a.grad = t->grad;
-  a.log_a = ctx->adj_log_a;
-  a.log_b = ctx->adj_log_b;
-  a.log_cell = ctx->adj_log_cell;
-  a.long_list = t->long_list;
-  a.long_G = t->long_G;
-  a.n_long = reinterpret_cast<unsigned int *>(t->scalars + 1);
-  a.work = ctx->adj_work;
-  a.flags = reinterpret_cast<uint32_t *>(t->scalars + 2);
-  a.n = t->n;
-  a.visit_bound = visit_bound;
-  a.scale = scale;
-  a.log_len = ctx->adj_log_len;
-  CellsDev c{};
-  c.xs = t->xs;
-  c.group_v = t->group_v;
-  BGS_CUDA(ctx, cudaEventRecord(ctx->ev0, s));
-  launch_adjoint_replay(ctx->mesh, c, t->bank, a, t->seed, ctx->adj_shape, s);
-  BGS_LAUNCHED(ctx, 3);
-  BGS_CUDA(ctx, cudaEventRecord(ctx->ev1, s));
-  launch_adjoint_grad_to_double(nc, t->grad, scale, t->grad_out, s);
-  BGS_LAUNCHED(ctx, 1);
-  BGS_CUDA(ctx, cudaMemcpyAsync(grad_sigma_a, t->grad_out, nc * sizeof(double), cudaMemcpyDeviceToHost, s));
-  unsigned long long sc[2];
-  BGS_CUDA(ctx, cudaMemcpyAsync(sc, t->scalars + 1, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-  BGS_CUDA(ctx, cudaStreamSynchronize(s));
-  float ms = 0.0f;
-  BGS_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-  t->info.n_long = sc[0];
-  t->info.grad_scale = scale;
-  t->info.device_flags = (uint32_t)sc[1];
-  t->info.visit_bound = visit_bound;
-  t->info.replay_ms = ms;
-  if (sc[1]) return check_flags(ctx, (uint32_t)sc[1]);
+int bgs_batch_adjoint_backward(bgs_batch *b, bgs_adjoint_tape *const *tapes, const double *const *grad_abs_E,
+                               double *const *grad_sigma_a) {
+  if (!b || !tapes || !grad_abs_E || !grad_sigma_a) return BGS_ERR_INVALID;
+  int rc = bgs_batch_synchronize(b);
+  if (rc) return rc;
+  const std::vector<bgs_context *> &ctx = batch_contexts(b);
+  rc = replay_backward(ctx[0], ctx.data(), tapes, (uint32_t)ctx.size(), grad_abs_E, grad_sigma_a);
+  if (rc) return batch_fail(b, rc, ctx[0]->err);
   return BGS_OK;
 }
 

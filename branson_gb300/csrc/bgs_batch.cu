@@ -69,17 +69,6 @@ __global__ void __launch_bounds__(kItemThreads) k_batch_items(const ProblemView 
   }
 }
 
-// problem of item w: the last p with item_off[p] <= w
-__device__ __forceinline__ uint32_t problem_of(const unsigned long long *item_off, uint32_t n,
-                                               unsigned long long w) {
-  uint32_t lo = 0, hi = n;
-  while (hi - lo > 1) {
-    const uint32_t mid = (lo + hi) >> 1;
-    if (item_off[mid] <= w) lo = mid; else hi = mid;
-  }
-  return lo;
-}
-
 __device__ __forceinline__ void flush_batched(const ProblemView &P, uint32_t cell, double a, double t,
                                               uint32_t &flags) {
   const DeviceDiag *d = P.d;

@@ -117,6 +117,10 @@ int read_transport_time(bgs_batch *b) {
 
 }  // namespace
 
+const std::vector<bgs_context *> &batch_contexts(const bgs_batch *b) { return b->ctx; }
+
+int batch_fail(bgs_batch *b, int code, const std::string &msg) { return bfail(b, code, "%s", msg.c_str()); }
+
 extern "C" {
 
 int bgs_batch_create(bgs_batch **out, uint32_t n, bgs_context *const *contexts) {

@@ -53,7 +53,15 @@ struct bgs_context {
   uint32_t adj_log_len = 256;          // cell visits one replay thread logs
   double *adj_log_a = nullptr, *adj_log_b = nullptr;
   uint32_t *adj_log_cell = nullptr;
-  unsigned long long *adj_work = nullptr;
+  unsigned long long *adj_work = nullptr;          // [0] queue head, [1] long-history count, [2] flags
+  unsigned long long *adj_long_list = nullptr;     // long histories (work items)
+  double *adj_long_G = nullptr;
+  unsigned long long adj_items_cap = 0;
+  AdjProblem *adj_probs = nullptr;                 // replay problem table and item offsets
+  unsigned long long *adj_item_off = nullptr;
+  uint32_t adj_probs_cap = 0;
+  std::vector<AdjProblem> h_adj_probs;
+  std::vector<unsigned long long> h_adj_item_off;
   unsigned long long mesh_generation = 0;  // bumped by every bgs_set_mesh
 
   DeviceDiag *d_diag = nullptr;
@@ -143,5 +151,10 @@ inline int read_diag(bgs_context *ctx) {
 // compaction into the other bank (which becomes current) and the tallies
 // converted to doubles.
 int prepare_transport(bgs_context *ctx, const Bank &from);
+
+// a batch's contexts in problem order, and its error message (bgs_batch_api.cu)
+struct bgs_batch;
+const std::vector<bgs_context *> &batch_contexts(const bgs_batch *b);
+int batch_fail(bgs_batch *b, int code, const std::string &msg);
 int run_transport(bgs_context *ctx, const Bank &from, uint32_t algorithm);
 int finish_transport(bgs_context *ctx, double next_dt);

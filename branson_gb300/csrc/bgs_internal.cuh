@@ -111,21 +111,32 @@ struct __align__(32) AdjCell {
   double w, f2, g2, inv_se;
 };
 
-struct AdjointDev {
+// One problem of an adjoint replay launch (bgs_adjoint.cu): its mesh, the
+// saved step (start states, transport table, adjoint coefficients), its
+// gradient sums and their fixed-point range.
+struct AdjProblem {
+  MeshDev m;
+  const CellXS *xs;
+  const double *group_v;
+  Bank t;                         // start states saved by the forward
   const AdjCell *cell;
   const double *src;              // f/sigma_a: d ln(emission weight)/d sigma_a per cell
   unsigned long long *grad;       // per cell (lo, hi): 128-bit two's-complement fixed point
+  unsigned long long seed_hi;
+  double visit_bound;             // |contribution of one visit| above this is a range error
+  int scale;                      // fixed-point exponent of the gradient sums
+};
+
+// Scratch shared by all problems of a replay launch.
+struct AdjShared {
   double *log_a, *log_b;          // per-thread visit logs, log_len entries each
   uint32_t *log_cell;
-  uint32_t *long_list;            // histories with more visits than a log holds
+  uint32_t log_len;
+  unsigned long long *long_list;  // work items (over all problems) with more visits than a log holds
   double *long_G;                 // their totals (second replay)
   unsigned int *n_long;
   unsigned long long *work;       // work-queue head
   uint32_t *flags;
-  unsigned long long n;           // histories on the tape
-  double visit_bound;             // |contribution of one visit| above this is a range error
-  int scale;                      // fixed-point exponent of the gradient sums
-  uint32_t log_len;
 };
 
 // Scalars of one step kept on the device (so a step never waits for the host).

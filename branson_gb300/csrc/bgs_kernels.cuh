@@ -119,6 +119,17 @@ void launch_event_init(const EventState &es, DeviceDiag *d, cudaStream_t s);
 void launch_event_round(const MeshDev &m, const CellsDev &c, const Bank &b, DeviceDiag *d, uint32_t seed,
                         const EventState &es, bool first, int n_sm, cudaStream_t s);
 
+// problem of work item w: the last p with item_off[p] <= w (n problems)
+__device__ __forceinline__ uint32_t problem_of(const unsigned long long *item_off, uint32_t n,
+                                               unsigned long long w) {
+  uint32_t lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (item_off[mid] <= w) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
 // Many independent problems stepped together (bgs_batch.cu): one problem's
 // view for the batched launches, in device memory.  Every batched kernel
 // takes the view table and runs problem blockIdx.y; the step's parameters
@@ -162,8 +173,10 @@ TransportLaunch adjoint_launch_shape(int n_sm);
 void launch_adjoint_cells(const CellsDev &c, uint32_t n_cells, AdjCell *adj, double *src,
                           unsigned long long *coef_max_bits, cudaStream_t s);
 void launch_adjoint_set_w(uint32_t n_cells, AdjCell *adj, const double *w, cudaStream_t s);
-void launch_adjoint_replay(const MeshDev &m, const CellsDev &c, const Bank &tape, const AdjointDev &a,
-                           uint32_t seed, const TransportLaunch &shape, cudaStream_t s);
+// the replay passes over n problems; item_off (device, n+1 entries) is the
+// exclusive prefix sum of the problems' saved histories
+void launch_adjoint_replay(const AdjProblem *probs, uint32_t n, const unsigned long long *item_off,
+                           const AdjShared &a, const TransportLaunch &shape, cudaStream_t s);
 void launch_adjoint_grad_to_double(uint32_t n_cells, const unsigned long long *grad, int scale, double *out,
                                    cudaStream_t s);
 

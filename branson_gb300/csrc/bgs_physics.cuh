@@ -117,6 +117,54 @@ __device__ __forceinline__ void flush_tally(const CellsDev &c, const DeviceDiag 
   }
 }
 
+// Warp-aggregated tally flush: every lane of the warp calls it (flush false
+// for lanes with nothing to add); lanes flushing into the same cell
+// (__match_any_sync on the cell, or on problem<<32|cell for the batched
+// kernel) add their 128-bit fixed-point contributions by shuffles and one
+// lane per cell issues the atomics.  Fixed-point sums are exact, so the
+// tallies are the same bits as with one atomic per lane; few-cell meshes
+// (where many lanes hit one cell) need far fewer atomics.
+__device__ __forceinline__ void add128(unsigned long long &lo, unsigned long long &hi, unsigned long long vlo,
+                                       unsigned long long vhi) {
+  lo += vlo;
+  hi += vhi + (lo < vlo ? 1ULL : 0ULL);
+}
+
+template <typename Key>
+__device__ __forceinline__ void flush_tally_warp(TallyCell *tally, bool flush, Key key, uint32_t cell, double a,
+                                                 double t, uint32_t &flags, int sa, int st) {
+  if (!__any_sync(0xffffffffu, flush)) return;
+  unsigned long long alo = 0, ahi = 0, tlo = 0, thi = 0;
+  if (flush) {
+    if ((__double_as_longlong(a) << 1) != 0 && !to_fixed128(a, sa, alo, ahi)) {
+      flags |= (a == a) ? FLAG_TALLY_RANGE : FLAG_NAN;
+      alo = ahi = 0;
+    }
+    if ((__double_as_longlong(t) << 1) != 0 && !to_fixed128(t, st, tlo, thi)) {
+      flags |= (t == t) ? FLAG_TALLY_RANGE : FLAG_NAN;
+      tlo = thi = 0;
+    }
+  }
+  const unsigned grp = __match_any_sync(0xffffffffu, flush ? key : (Key)~(Key)0);
+  if (!flush) return;
+  if (grp & (grp - 1)) {  // several lanes on this cell: sum into the first
+    unsigned long long s_alo = 0, s_ahi = 0, s_tlo = 0, s_thi = 0;
+    unsigned mm = grp;
+    while (mm) {
+      const int m = __ffs(mm) - 1;
+      mm &= mm - 1;
+      add128(s_alo, s_ahi, __shfl_sync(grp, alo, m), __shfl_sync(grp, ahi, m));
+      add128(s_tlo, s_thi, __shfl_sync(grp, tlo, m), __shfl_sync(grp, thi, m));
+    }
+    alo = s_alo; ahi = s_ahi; tlo = s_tlo; thi = s_thi;
+  }
+  if ((int)(threadIdx.x & 31u) == __ffs(grp) - 1) {
+    TallyCell *tc = &tally[cell];
+    if (alo | ahi) atomic_add128(&tc->abs_lo, &tc->abs_hi, alo, ahi);
+    if (tlo | thi) atomic_add128(&tc->trk_lo, &tc->trk_hi, tlo, thi);
+  }
+}
+
 __device__ __forceinline__ void direction_recips(Lane &L) {
 #if BGS_INT_DIV
   L.rbx = fix::divisor_recip(L.dx);

@@ -81,37 +81,48 @@ __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
       }
     }
     if (__all_sync(0xffffffffu, !active)) break;
-    if (!active) continue;
 
-    // ---- one segment of transport_photon (history_based_transport.h:55-139)
-    ++seg_total;
-    const CellXS xs = c.xs[L.cell];
-    uint32_t surface_cross;
-    const int ev = segment_advance(xs, L, surface_cross, flags);
-    if (ev == SEG_KILLED) {
-      flush_tally(c, d, L.cell, L.thr_abs, L.thr_trk, flags, sa, st);
-      store_end(b, L, KILLED);
-      active = false;
-    } else if (ev == SEG_SCATTER) {
-      scatter_update(m, c, xs, L);
-    } else if (ev == SEG_BOUNDARY) {
-      const int bc = face_bc(m, L, surface_cross);
-      if (bc == ELEMENT) {
-        flush_tally(c, d, L.cell, L.thr_abs, visit_track(xs, L, ev), flags, sa, st);
-        L.thr_abs = 0.0;
-        enter_neighbour(m, L, surface_cross);
-      } else if (bc == VACUUM || bc == SOURCE || bc == PROCESSOR) {
-        flush_tally(c, d, L.cell, L.thr_abs, visit_track(xs, L, ev), flags, sa, st);
-        store_end(b, L, bc == PROCESSOR ? PASS : EXIT);
-        active = false;
+    // ---- one segment of transport_photon (history_based_transport.h:55-139);
+    // every flush of the loop trip goes through one warp-wide aggregated
+    // flush after the event handling (lanes without a history take part
+    // with nothing to add)
+    bool flush = false;
+    uint32_t fcell = 0;
+    double fa = 0.0, ft = 0.0;
+    if (active) {
+      ++seg_total;
+      const CellXS xs = c.xs[L.cell];
+      uint32_t surface_cross;
+      const int ev = segment_advance(xs, L, surface_cross, flags);
+      if (ev == SEG_SCATTER) {
+        scatter_update(m, c, xs, L);
       } else {
-        reflect(m, L, surface_cross);
+        int bc = ELEMENT;
+        if (ev == SEG_BOUNDARY) bc = face_bc(m, L, surface_cross);
+        if (ev != SEG_BOUNDARY || bc != REFLECT) {  // the visit to this cell ends
+          flush = true;
+          fcell = L.cell;
+          fa = L.thr_abs;
+          ft = visit_track(xs, L, ev);
+        }
+        if (ev == SEG_KILLED) {
+          store_end(b, L, KILLED);
+          active = false;
+        } else if (ev == SEG_CENSUS) {
+          store_end(b, L, CENSUS);
+          active = false;
+        } else if (bc == ELEMENT) {
+          L.thr_abs = 0.0;
+          enter_neighbour(m, L, surface_cross);
+        } else if (bc == VACUUM || bc == SOURCE || bc == PROCESSOR) {
+          store_end(b, L, bc == PROCESSOR ? PASS : EXIT);
+          active = false;
+        } else {
+          reflect(m, L, surface_cross);
+        }
       }
-    } else {  // SEG_CENSUS
-      flush_tally(c, d, L.cell, L.thr_abs, visit_track(xs, L, ev), flags, sa, st);
-      store_end(b, L, CENSUS);
-      active = false;
     }
+    flush_tally_warp(c.tally, flush, fcell, fcell, fa, ft, flags, sa, st);
   }
 
   // ---- per-warp totals

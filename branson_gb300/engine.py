@@ -49,6 +49,7 @@ class ReplicatedIMC:
         self.lib = _lib.load()
         self.deck = deck
         self.device = device
+        self.algorithm = deck.algorithm  # HISTORY or EVENT for step(); the tuner may change it
         deck.validate()
         self.capacity = int(capacity or default_capacity(deck))
         ctx = C.c_void_p()
@@ -114,8 +115,11 @@ class ReplicatedIMC:
         self.dt = nd
         self.step_no += 1
 
-    def step(self, algorithm: int = _lib.HISTORY, sync: bool = True) -> Optional[StepReport]:
-        """One replicated IMC time step on the device (bgs_step)."""
+    def step(self, algorithm: Optional[int] = None, sync: bool = True) -> Optional[StepReport]:
+        """One replicated IMC time step on the device (bgs_step), in the given
+        algorithm or the context's (the deck's, or the tuner's choice)."""
+        if algorithm is None:
+            algorithm = self.algorithm
         nd = self.next_dt()
         if nd <= 0.0:  # past t_stop: keep stepping with the current dt
             nd = self.dt
@@ -142,7 +146,8 @@ class ReplicatedIMC:
     def source(self, step: int, dt: float) -> None:
         self._check(self.lib.bgs_source(self.ctx, step, dt), "bgs_source")
 
-    def transport(self, next_dt: float, algorithm: int = _lib.HISTORY) -> Dict[str, float]:
+    def transport(self, next_dt: float, algorithm: Optional[int] = None) -> Dict[str, float]:
+        algorithm = self.algorithm if algorithm is None else algorithm
         t = _lib.TransportDiag()
         self._check(self.lib.bgs_transport(self.ctx, next_dt, algorithm, C.byref(t)), "bgs_transport")
         return {k: getattr(t, k) for k, _ in _lib.TransportDiag._fields_}
@@ -181,11 +186,12 @@ class ReplicatedIMC:
         s = ph.struct()
         self._check(self.lib.bgs_set_photons(self.ctx, ph.n, C.byref(s)), "bgs_set_photons")
 
-    def replicated_transport(self, ph: PhotonArrays, next_dt: float, algorithm: int = _lib.HISTORY,
+    def replicated_transport(self, ph: PhotonArrays, next_dt: float, algorithm: Optional[int] = None,
                              census: Optional[PhotonArrays] = None):
         """Drop-in replicated_transport on host buffers: ``ph`` is updated in
         place with the end states; returns (abs_E, track_E, census, census_E,
         exit_E) with the census in input order."""
+        algorithm = self.algorithm if algorithm is None else algorithm
         abs_E = np.empty(self.n_cells)
         track_E = np.empty(self.n_cells)
         if census is None:

@@ -58,8 +58,10 @@ def default_candidates() -> List[Schedule]:
 
 
 def apply(imc: ReplicatedIMC, s: Schedule, n_sm: int, blocks_per_sm: Optional[int] = None) -> None:
-    """Set a schedule on a context.  grid_fraction < 1 shrinks the occupancy
-    grid (blocks_per_sm blocks per SM for the chosen block size)."""
+    """Set a schedule on a context (its step() then runs in the schedule's
+    algorithm).  grid_fraction < 1 shrinks the occupancy grid (blocks_per_sm
+    blocks per SM for the chosen block size)."""
+    imc.algorithm = s.algorithm
     imc.set_option("transport_threads", s.threads)
     if s.grid_fraction >= 1.0 or blocks_per_sm is None:
         imc.set_option("transport_blocks", 0)
@@ -70,9 +72,9 @@ def apply(imc: ReplicatedIMC, s: Schedule, n_sm: int, blocks_per_sm: Optional[in
 
 
 def _blocks_per_sm(threads: int) -> int:
-    # the history kernel keeps the register budget of five 128-thread blocks
+    # the history kernel keeps the register budget of six 128-thread blocks
     # per SM for every block size (launch bounds in bgs_transport.cu)
-    return max(1, (5 * 128) // threads)
+    return max(1, (6 * 128) // threads)
 
 
 def tune(imc: ReplicatedIMC, candidates: Optional[Sequence[Schedule]] = None, repeats: int = 3,

@@ -296,6 +296,16 @@ BGS_API const char *bgs_batch_last_error(const bgs_batch *batch);
 BGS_API int bgs_batch_step(bgs_batch *batch, const bgs_step_params *params, bgs_transport_diag *out);
 BGS_API int bgs_batch_synchronize(bgs_batch *batch);
 BGS_API int bgs_batch_set_option(bgs_batch *batch, int option, double value);
+/* Adjoint of a batch's current step (see bgs_adjoint_forward / _backward):
+ * the forward runs per problem (arrays of n entries: sigma_a[i] and
+ * counts[i] may be NULL, or the arrays themselves NULL; tapes[i] as in
+ * bgs_adjoint_forward); the backward replays every problem's tape in one
+ * persistent launch (work items: all problems' saved histories) and writes
+ * grad_sigma_a[i] for each.  The results equal the per-problem calls. */
+BGS_API int bgs_batch_adjoint_forward(bgs_batch *batch, const bgs_step_params *params, const double *const *sigma_a,
+                                      const uint32_t *const *counts, double *const *abs_E, bgs_adjoint_tape **tapes);
+BGS_API int bgs_batch_adjoint_backward(bgs_batch *batch, bgs_adjoint_tape *const *tapes,
+                                       const double *const *grad_abs_E, double *const *grad_sigma_a);
 /* Device time (ms) of the last batched transport launch, and the kernels
  * the batch has launched (its own and the contexts' phases). */
 BGS_API int bgs_batch_last_transport_ms(bgs_batch *batch, float *ms, uint64_t *kernel_launches);

@@ -72,3 +72,30 @@ def test_batch_rejects_bad_arguments(gpu_lib):
         assert lib.bgs_batch_create(C.byref(h), 0, same) == _lib.ERR_INVALID
     finally:
         imc.close()
+
+
+def test_batched_adjoint_equals_per_problem(gpu_lib):
+    """One replay launch over every problem's tape gives each problem's
+    gradient bit for bit as its own backward does."""
+    from branson_gb300 import deck as D
+    from branson_gb300.adjoint import batch_backward, batch_forward
+    from branson_gb300.engine import BatchIMC
+
+    decks = [D.random_opacity_cube(n_per_axis=n, photons=p, seed=s)
+             for n, p, s in ((4, 3000, 1), (6, 12000, 2), (8, 20000, 3))]
+    decks += [D.hot_zone(n_per_axis=10, photons=15000, n_steps=2)]
+    decks += D.batch_ensemble(n_problems=3, master_seed=5, side_range=(4, 10), photon_median=4000,
+                              photon_range=(1000, 9000))
+    rng = np.random.default_rng(0)
+    with BatchIMC(decks) as batch:
+        abs_E, tapes = batch_forward(batch)
+        ws = [rng.uniform(-1.0, 1.0, p.n_cells) for p in batch.problems]
+        grads = batch_backward(batch, tapes, ws)
+        for i, (p, t, w) in enumerate(zip(batch.problems, tapes, ws)):
+            own = np.empty(p.n_cells)
+            rc = batch.lib.bgs_adjoint_backward(p.ctx, t.handle, w.ctypes.data, own.ctypes.data)
+            assert rc == 0, p.lib.bgs_last_error(p.ctx)
+            np.testing.assert_array_equal(grads[i], own, err_msg=f"problem {i}")
+            assert np.any(own != 0.0)
+        for t in tapes:
+            t.close()
