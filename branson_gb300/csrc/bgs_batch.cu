@@ -69,13 +69,11 @@ __global__ void __launch_bounds__(kItemThreads) k_batch_items(const ProblemView 
   }
 }
 
-__device__ __forceinline__ void flush_batched(const ProblemView &P, uint32_t cell, double a, double t,
-                                              uint32_t &flags) {
-  const DeviceDiag *d = P.d;
-  flush_tally(P.c, d, cell, a, t, flags, d->scale_abs, d->scale_track);
-}
+#ifndef BGS_BATCH_MIN_BLOCKS
+#define BGS_BATCH_MIN_BLOCKS 5
+#endif
 
-__global__ void __launch_bounds__(kTransportThreads, BGS_MIN_BLOCKS)
+__global__ void __launch_bounds__(kTransportThreads, BGS_BATCH_MIN_BLOCKS)
     k_transport_batched(const ProblemView *__restrict__ probs, uint32_t n_probs,
                         const unsigned long long *__restrict__ item_off, unsigned long long *work_counter) {
   const unsigned long long n = item_off[n_probs];
@@ -126,45 +124,54 @@ __global__ void __launch_bounds__(kTransportThreads, BGS_MIN_BLOCKS)
       }
     }
     if (__all_sync(0xffffffffu, !active)) break;
-    if (!active) continue;
 
-    // ---- one segment of transport_photon (history_based_transport.h:55-139)
-    const CellXS xs = xs_p[L.cell];
-    uint32_t surface_cross;
-    const int ev = segment_advance(xs, L, surface_cross, flags);
-    bool end = false;
-    uint8_t desc = KILLED;
-    if (ev == SEG_KILLED) {
-      end = true;
-    } else if (ev == SEG_SCATTER) {
-      scatter_update(probs[p].m, probs[p].c, xs, L);
-    } else if (ev == SEG_BOUNDARY) {
-      const MeshDev &m = probs[p].m;
-      const int bc = face_bc(m, L, surface_cross);
-      if (bc == ELEMENT) {
-        flush_batched(probs[p], L.cell, L.thr_abs, visit_track(xs, L, ev), flags);
-        L.thr_abs = 0.0;
-        enter_neighbour(m, L, surface_cross);
-      } else if (bc == VACUUM || bc == SOURCE || bc == PROCESSOR) {
-        end = true;
-        desc = bc == PROCESSOR ? PASS : EXIT;
+    // ---- one segment of transport_photon (history_based_transport.h:55-139);
+    // flushes go through one warp-wide aggregated flush keyed on
+    // (problem, cell), as in k_transport_history
+    bool flush = false, ended = false;
+    uint32_t fcell = 0;
+    double fa = 0.0, ft = 0.0;
+    if (active) {
+      const CellXS xs = xs_p[L.cell];
+      uint32_t surface_cross;
+      const int ev = segment_advance(xs, L, surface_cross, flags);
+      if (ev == SEG_SCATTER) {
+        scatter_update(probs[p].m, probs[p].c, xs, L);
       } else {
-        reflect(m, L, surface_cross);
+        const MeshDev &m = probs[p].m;
+        int bc = ELEMENT;
+        if (ev == SEG_BOUNDARY) bc = face_bc(m, L, surface_cross);
+        if (ev != SEG_BOUNDARY || bc != REFLECT) {  // the visit to this cell ends
+          flush = true;
+          fcell = L.cell;
+          fa = L.thr_abs;
+          ft = visit_track(xs, L, ev);
+        }
+        if (ev == SEG_KILLED || ev == SEG_CENSUS || bc == VACUUM || bc == SOURCE || bc == PROCESSOR) {
+          const uint8_t desc = ev == SEG_KILLED ? KILLED
+                             : ev == SEG_CENSUS ? CENSUS : (bc == PROCESSOR ? PASS : EXIT);
+          store_end(probs[p].from, L, desc);
+          ended = true;
+        } else if (bc == ELEMENT) {
+          L.thr_abs = 0.0;
+          enter_neighbour(m, L, surface_cross);
+        } else {
+          reflect(m, L, surface_cross);
+        }
       }
-    } else {  // SEG_CENSUS
-      end = true;
-      desc = CENSUS;
     }
-    if (end) {
+    {
       const ProblemView &P = probs[p];
-      flush_batched(P, L.cell, L.thr_abs, visit_track(xs, L, ev), flags);
-      store_end(P.from, L, desc);
-      atomicAdd(&P.d->n_segments, (unsigned long long)L.segs);
-      if (flags) {
-        atomicOr(&P.d->flags, flags);
-        flags = 0;
+      const int sa = flush ? P.d->scale_abs : 0, st = flush ? P.d->scale_track : 0;
+      flush_tally_warp(P.c.tally, flush, ((unsigned long long)p << 32) | fcell, fcell, fa, ft, flags, sa, st);
+      if (ended) {
+        atomicAdd(&P.d->n_segments, (unsigned long long)L.segs);
+        if (flags) {
+          atomicOr(&P.d->flags, flags);
+          flags = 0;
+        }
+        active = false;
       }
-      active = false;
     }
   }
   __syncthreads();

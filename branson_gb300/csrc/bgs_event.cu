@@ -72,6 +72,9 @@ __global__ void __launch_bounds__(kEventThreads) k_event_advance(MeshDev m, Cell
     const unsigned int w = w0 + (threadIdx.x & 31u);
     int ev = -1;
     uint32_t p = 0, sc = 0;
+    bool flush = false;
+    uint32_t fcell = 0;
+    double fa = 0.0, ft = 0.0;
     if (w < n) {
       p = es.active[w];
       Lane L;
@@ -84,7 +87,10 @@ __global__ void __launch_bounds__(kEventThreads) k_event_advance(MeshDev m, Cell
         const CellXS xs = c.xs[L.cell];
         ev = segment_advance(xs, L, sc, flags);
         if (ev == SEG_KILLED || ev == SEG_CENSUS) {
-          flush_tally(c, d, L.cell, L.thr_abs, visit_track(xs, L, ev), flags, sa, st);
+          flush = true;
+          fcell = L.cell;
+          fa = L.thr_abs;
+          ft = visit_track(xs, L, ev);
           store_end(b, L, ev == SEG_KILLED ? KILLED : CENSUS);
         } else {
           b.px[p] = L.px; b.py[p] = L.py; b.pz[p] = L.pz;
@@ -94,6 +100,7 @@ __global__ void __launch_bounds__(kEventThreads) k_event_advance(MeshDev m, Cell
         }
       }
     }
+    flush_tally_warp(c.tally, flush, fcell, fcell, fa, ft, flags, sa, st);
     queue_push(ev == SEG_SCATTER, p, es.q_scatter, es.n_scatter);
     queue_push(ev == SEG_BOUNDARY, p, es.q_boundary, es.n_boundary);
   }
@@ -144,6 +151,9 @@ __global__ void __launch_bounds__(kEventThreads) k_event_boundary(MeshDev m, Cel
     const unsigned int w = w0 + (threadIdx.x & 31u);
     uint32_t p = 0;
     bool survive = false;
+    bool flush = false;
+    uint32_t fcell = 0;
+    double fa = 0.0;
     if (w < n) {
       p = es.q_boundary[w];
       Lane L;
@@ -151,9 +161,12 @@ __global__ void __launch_bounds__(kEventThreads) k_event_boundary(MeshDev m, Cel
       L.ci = L.cell % m.ngx; L.cj = (L.cell / m.ngx) % m.ngy; L.ck = L.cell / (m.ngx * m.ngy);
       const uint32_t sc = es.surface[p];
       const int bc = face_bc(m, L, sc);
+      if (bc == ELEMENT || bc == VACUUM || bc == SOURCE || bc == PROCESSOR) {  // the visit ends
+        flush = true;
+        fcell = L.cell;
+        fa = es.thr_abs[p];
+      }
       if (bc == ELEMENT) {
-        const double a = es.thr_abs[p];
-        flush_tally(c, d, L.cell, a, a * c.xs[L.cell].inv_saf, flags, sa, st);
         es.thr_abs[p] = 0.0;
         switch (sc) {
           case 0: L.cell -= 1; break;
@@ -166,8 +179,6 @@ __global__ void __launch_bounds__(kEventThreads) k_event_boundary(MeshDev m, Cel
         b.cell[p] = L.cell;
         survive = true;
       } else if (bc == VACUUM || bc == SOURCE || bc == PROCESSOR) {
-        const double a = es.thr_abs[p];
-        flush_tally(c, d, L.cell, a, a * c.xs[L.cell].inv_saf, flags, sa, st);
         b.desc[p] = bc == PROCESSOR ? PASS : EXIT;
       } else {  // REFLECT (photon.h:151-155)
         if (sc < 2) b.dx[p] = -b.dx[p];
@@ -176,6 +187,7 @@ __global__ void __launch_bounds__(kEventThreads) k_event_boundary(MeshDev m, Cel
         survive = true;
       }
     }
+    flush_tally_warp(c.tally, flush, fcell, fcell, fa, flush ? fa * c.xs[fcell].inv_saf : 0.0, flags, sa, st);
     queue_push(survive, p, es.next, es.n_next);
   }
   for (int o = 16; o > 0; o >>= 1) flags |= __shfl_down_sync(0xffffffffu, flags, o);
