@@ -102,6 +102,10 @@ __global__ void k_reset_queue(DeviceDiag *d) {
   d->n_segments = 0;
 }
 
+// the history tail after event rounds restarts the work queue only; the
+// segments the event stages counted stay in the step's total
+__global__ void k_reset_work(DeviceDiag *d) { d->work_counter = 0; }
+
 }  // namespace
 
 // ===================================================================== C ABI
@@ -398,7 +402,7 @@ int transport_event(bgs_context *ctx, const Bank &from) {
   if (round == 0) {
     launch_transport_history(ctx->mesh, ctx->cells, from, ctx->d_diag, ctx->seed, ctx->tshape, ctx->stream);
   } else {
-    k_reset_queue<<<1, 1, 0, ctx->stream>>>(ctx->d_diag);
+    k_reset_work<<<1, 1, 0, ctx->stream>>>(ctx->d_diag);
     BGS_LAUNCHED(ctx, 1);
     launch_transport_resume(ctx->mesh, ctx->cells, from, ctx->d_diag, ctx->seed, tail_es, ctx->tshape,
                             ctx->stream);

@@ -33,6 +33,12 @@ constexpr int kTransportThreads = 128;
 #ifndef BGS_RECIP_DIV_DS
 #define BGS_RECIP_DIV_DS 1  // -log(u)/sigma_eff: division by the cell's stored reciprocal
 #endif
+#ifndef BGS_APPROX_FACES
+#define BGS_APPROX_FACES 1  // order the three face distances in single precision, divide once
+#endif
+#ifndef BGS_APPROX_CVT_HW
+#define BGS_APPROX_CVT_HW 0  // single-precision images by the conversion instruction (else by bits)
+#endif
 
 
 // a/b correctly rounded from y = RN(1/b): q0 = RN(a*y) is within one ulp of
@@ -228,6 +234,70 @@ __device__ __forceinline__ double visit_track(const CellXS &xs, const Lane &L, i
   return ev == SEG_KILLED ? L.thr_trk : L.thr_abs * xs.inv_saf;
 }
 
+// Single-precision image of a double, truncated (relative error below
+// 2^-23); false when |x| is nonzero and outside float's normal range.
+__device__ __forceinline__ bool f32_image(double x, float &f) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const bool zero = (u << 1) == 0;
+#if BGS_APPROX_CVT_HW
+  f = __double2float_rz(x);
+  const float m = fabsf(f);
+  return zero || (m >= 1.17549435e-38f && m < 3.0e38f);
+#else
+  const unsigned hi = (unsigned)(u >> 32), lo = (unsigned)u;
+  const unsigned mag = hi & 0x7FFFFFFFu;
+  // exponent field e in [897, 1150] is float's normal range: the float's
+  // exponent field is e - 896 and its 23 mantissa bits the double's top 23
+  const unsigned bits = __funnelshift_l(lo, mag - (896u << 20), 3) | (hi & 0x80000000u);
+  f = zero ? 0.0f : __uint_as_float(bits);
+  return zero || (mag - (897u << 20)) < ((1151u - 897u) << 20);
+#endif
+}
+
+// The face that get_distance_to_boundary picks (cell.h:117-132), decided
+// from single-precision quotients, with one double division for the
+// winner.  Each approximate quotient is within 2^-20 (relative) of the
+// correctly rounded one (two truncations below 2^-23 and __fdividef's two
+// ulps), so when the winner is separated from every other candidate by
+// more than 2^-18 of their magnitudes, and every quotient from the 1e16
+// limit by more than 1e-4 of it, the exact comparisons order them the same
+// way and the division returns the distance the three-division form would.  Anything
+// else (near ties, a zero or subnormal-range direction cosine, a quotient
+// near 1e16 or beyond float's range) returns false and the caller runs the
+// three exact divisions.
+__device__ __forceinline__ bool approx_faces(double ax, double ay, double az, const Lane &L, bool posx,
+                                             bool posy, bool posz, double &dist_to_boundary,
+                                             long long &k_boundary, uint32_t &surface_cross) {
+  float fax, fay, faz, fdx, fdy, fdz;
+  bool ok = f32_image(ax, fax) & f32_image(ay, fay) & f32_image(az, faz);
+  ok &= f32_image(L.dx, fdx) & f32_image(L.dy, fdy) & f32_image(L.dz, fdz);
+  ok &= (fdx != 0.0f) & (fdy != 0.0f) & (fdz != 0.0f);
+  const float qx = __fdividef(fax, fdx), qy = __fdividef(fay, fdy), qz = __fdividef(faz, fdz);
+  constexpr float kLo = 9.9999e15f, kHi = 1.0001e16f, kTol = 3.814697265625e-06f;  // 1e16 -+ 1e-4, 2^-18
+  const float kInf = __int_as_float(0x7f800000);
+  ok &= !(qx >= kLo && qx <= kHi) & !(qy >= kLo && qy <= kHi) & !(qz >= kLo && qz <= kHi);
+  const float cx = qx < kLo ? qx : kInf, cy = qy < kLo ? qy : kInf, cz = qz < kLo ? qz : kInf;
+  int j = 0;
+  float m = cx, second = fminf(cy, cz);
+  if (cy < m) { j = 1; m = cy; second = fminf(cx, cz); }
+  if (cz < m) { j = 2; m = cz; second = fminf(cx, cy); }
+  if (m != kInf) ok &= (second == kInf) || (second - m > kTol * (fabsf(second) + fabsf(m)));
+  if (!ok) return false;
+  if (m == kInf) {  // no face closer than 1e16
+    dist_to_boundary = 1.0e16;
+    k_boundary = f64_key(1.0e16);
+    surface_cross = 0;
+    return true;
+  }
+  const double a = j == 0 ? ax : (j == 1 ? ay : az);
+  const double b = j == 0 ? L.dx : (j == 1 ? L.dy : L.dz);
+  const bool pos = j == 0 ? posx : (j == 1 ? posy : posz);
+  dist_to_boundary = a / b;
+  k_boundary = f64_key(dist_to_boundary);
+  surface_cross = 2u * (uint32_t)j + (pos ? 1u : 0u);
+  return true;
+}
+
 // details of a segment the adjoint replay needs (unused elsewhere, so the
 // compiler drops them from the other kernels)
 struct SegInfo {
@@ -266,7 +336,11 @@ __device__ __forceinline__ int segment_advance(const CellXS &xs, Lane &L, uint32
   const double ax = L.fx - L.px;
   const double ay = L.fy - L.py;
   const double az = L.fz - L.pz;
-  {
+  bool decided = false;
+#if BGS_APPROX_FACES
+  decided = approx_faces(ax, ay, az, L, posx, posy, posz, dist_to_boundary, k_boundary, surface_cross);
+#endif
+  if (!decided) {
     double dist = seg_div(ax, L.dx, L.rbx);
     long long k = f64_key(dist);
     if (k < k_boundary) { dist_to_boundary = dist; k_boundary = k; surface_cross = posx ? 1u : 0u; }

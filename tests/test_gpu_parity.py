@@ -197,6 +197,24 @@ def test_event_mode_reproduces_history_mode(gpu_lib, name):
                         f"{name} event vs oracle")
 
 
+@pytest.mark.parametrize("name", ["hot_zone", "hohlraum30"])
+def test_event_mode_step_counts_every_segment(gpu_lib, name):
+    """A whole step in event mode (event rounds, then the history tail)
+    reports the segment count and fields of the same step in history mode."""
+    from branson_gb300 import _lib
+    from branson_gb300.engine import ReplicatedIMC
+
+    dk = _decks()[name]
+    with ReplicatedIMC(dk) as h, ReplicatedIMC(dk) as e:
+        e.set_option("event_round_cap", 4)
+        e.set_option("event_tail_fraction", 0.0)
+        rh, re_ = h.step(_lib.HISTORY), e.step(_lib.EVENT)
+        assert rh.n_segments > rh.n_transported > 0
+        assert (re_.n_transported, re_.n_census, re_.n_segments) == (rh.n_transported, rh.n_census, rh.n_segments)
+        for f in ("T_e", "abs_E", "track_E"):
+            np.testing.assert_array_equal(e.get_field(f), h.get_field(f))
+
+
 def _oracle_end(orc, photons, nd):
     ph = photons.copy()
     orc.transport(ph, nd)
