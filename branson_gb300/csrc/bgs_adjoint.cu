@@ -86,7 +86,13 @@ __global__ void __launch_bounds__(kAdjThreads, BGS_ADJ_MIN_BLOCKS)
         if (w < n) {
           item = w;
           gitem = kPass == 0 ? w : a.long_list[w];
-          p = problem_of(item_off, n_probs, gitem);
+          if (kPass == 0) {  // items only increase per lane: search forward from the last problem
+            uint32_t k = 0;
+            while (k < 4 && p + 1 < n_probs && item_off[p + 1] <= gitem) { ++p; ++k; }
+            if (k == 4) p = problem_of(item_off, n_probs, gitem, p);
+          } else {
+            p = problem_of(item_off, n_probs, gitem);
+          }
           const AdjProblem &P = probs[p];
           const Bank &t = P.t;
           const unsigned long long i = gitem - item_off[p];

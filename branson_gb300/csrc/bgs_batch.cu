@@ -7,7 +7,7 @@
 // bgs_transport.cu).  Work items are the concatenation of every problem's bank
 // (exclusive prefix sum of the problems' n_bank, formed on the device, so
 // no count goes through the host); each warp pulls items from one global
-// queue, a lane finds its problem by binary search at pickup and then runs
+// queue, a lane finds its problem at pickup (forward from its last one) and then runs
 // the history exactly as k_transport_history does (same per-segment code
 // from bgs_physics.cuh, the problem's seed, tallies and fixed-point scales),
 // so every problem's end states and tallies are those of its own launch.
@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(kItemThreads) k_batch_items(const ProblemView 
 }
 
 #ifndef BGS_BATCH_MIN_BLOCKS
-#define BGS_BATCH_MIN_BLOCKS 5
+#define BGS_BATCH_MIN_BLOCKS 6
 #endif
 
 __global__ void __launch_bounds__(kTransportThreads, BGS_BATCH_MIN_BLOCKS)
@@ -96,7 +96,12 @@ __global__ void __launch_bounds__(kTransportThreads, BGS_BATCH_MIN_BLOCKS)
       if (!active && !done) {
         const unsigned long long w = base + __popc(need & lanemask_lt);
         if (w < n) {
-          p = problem_of(item_off, n_probs, w);
+          // a lane's items only increase (the queue head only moves up), so
+          // its problem is at or after the last one: a few steps forward,
+          // else a binary search over the rest
+          uint32_t k = 0;
+          while (k < 4 && p + 1 < n_probs && item_off[p + 1] <= w) { ++p; ++k; }
+          if (k == 4) p = problem_of(item_off, n_probs, w, p);
           const ProblemView &P = probs[p];
           const unsigned long long i = w - item_off[p];
           const Bank &b = P.from;

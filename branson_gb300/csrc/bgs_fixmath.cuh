@@ -30,6 +30,10 @@
 
 #include "bgs_fixmath_tables.h"
 
+#ifndef BGS_FIX_NOINLINE
+#define BGS_FIX_NOINLINE 0
+#endif
+
 #if defined(__CUDACC__)
 #define BGS_HD __host__ __device__ __forceinline__
 // one shared copy in device code: routines called from several places of
@@ -39,6 +43,13 @@
 #else
 #define BGS_HD inline
 #define BGS_HD_SHARED inline
+#endif
+// the per-segment routines (log, exp, sin/cos, sqrt): inlined, or one
+// out-of-line copy each
+#if BGS_FIX_NOINLINE
+#define BGS_HD_ROUTINE BGS_HD_SHARED
+#else
+#define BGS_HD_ROUTINE BGS_HD
 #endif
 
 namespace bgs {
@@ -145,7 +156,7 @@ BGS_HD_SHARED double round_u128(u128 W, int scale) {
 // -ln(u) for the RNG draw u = m * 2^-53 (u01fixedpt: m odd, 1 <= m < 2^53).
 // The result is the value -log(u) rounds to (the upstream distance to
 // collision numerator, history_based_transport.h:62-63).
-BGS_HD double neg_log_u53(uint64_t m) {
+BGS_HD_ROUTINE double neg_log_u53(uint64_t m) {
   const uint64_t n = (1ULL << 53) - m;  // v = 1 - u = n * 2^-53, exact
   if (n < (1ULL << 42)) {
     // v < 2^-11: -ln(1-v) = v (1 + v/2 + v^2/3 + v^3/4 + v^4/5 + v^5/6), V = v*2^64
@@ -186,7 +197,7 @@ BGS_HD double neg_log_u53(uint64_t m) {
 // exp(-tau) for tau >= 0: the factor exp(-sigma_a*f*d) of the implicit-capture
 // weight decay (history_based_transport.h:74).  tau above 700 (result below
 // 1e-304) returns the CUDA/libm value instead of the fixed-point path.
-BGS_HD double exp_neg(double tau) {
+BGS_HD_ROUTINE double exp_neg(double tau) {
   const uint64_t tb = double_to_bits(tau);
   const int te = (int)((tb >> 52) & 0x7FF);
   if (te == 0) return 1.0;  // tau = 0 (or subnormal: exp rounds to 1)
@@ -242,7 +253,11 @@ BGS_HD double round_u64_scaled(uint64_t mant_hi, uint64_t mant_lo, int scale) {
   return round_u128(((u128)mant_hi << 64) | mant_lo, scale);
 }
 
-BGS_HD void sincos_phi(double phi, double *s_out, double *c_out) {
+struct SinCos {
+  double s, c;
+};
+
+BGS_HD_ROUTINE SinCos sincos_phi_v(double phi) {
   constexpr uint64_t kS[10] = {BGS_SIN_COEF_INIT};
   constexpr uint64_t kCo[10] = {BGS_COS_COEF_INIT};
   const uint64_t pb = double_to_bits(phi);
@@ -250,13 +265,14 @@ BGS_HD void sincos_phi(double phi, double *s_out, double *c_out) {
   // 0 < phi < 8 by the bit pattern (8.0 is 0x4020000000000000; a set sign
   // bit, a NaN or a zero/subnormal exponent all fall outside)
   if (be == 0 || pb >= 0x4020000000000000ULL) {
+    SinCos r;
 #if defined(__CUDA_ARCH__)
-    sincos(phi, s_out, c_out);
+    sincos(phi, &r.s, &r.c);
 #else
-    *s_out = std::sin(phi);
-    *c_out = std::cos(phi);
+    r.s = std::sin(phi);
+    r.c = std::cos(phi);
 #endif
-    return;
+    return r;
   }
   const int e = be - 1023;  // phi = M * 2^(e - 52), e <= 2
   const uint64_t M = (pb & 0x000FFFFFFFFFFFFFULL) | 0x0010000000000000ULL;
@@ -311,11 +327,17 @@ BGS_HD void sincos_phi(double phi, double *s_out, double *c_out) {
   const double so = swap ? cv : sv;  // sin, cos of (t*pi/2)
   const double co = swap ? sv : cv;
   switch (quad) {
-    case 0: *s_out = so; *c_out = co; break;
-    case 1: *s_out = co; *c_out = -so; break;
-    case 2: *s_out = -so; *c_out = -co; break;
-    default: *s_out = -co; *c_out = so; break;
+    case 0: return {so, co};
+    case 1: return {co, -so};
+    case 2: return {-so, -co};
+    default: return {-co, so};
   }
+}
+
+BGS_HD void sincos_phi(double phi, double *s_out, double *c_out) {
+  const SinCos r = sincos_phi_v(phi);
+  *s_out = r.s;
+  *c_out = r.c;
 }
 
 
@@ -441,7 +463,7 @@ BGS_HD double div_rn(double a, double b, uint64_t rb) {
 // sqrt(x) rounded to nearest for normal x > 0: 1/sqrt by Newton in fixed
 // point from a float seed, the root w*r, then the exact floor and rounding
 // checked with 128-bit integer squares.
-BGS_HD double sqrt_rn(double x) {
+BGS_HD_ROUTINE double sqrt_rn(double x) {
   const uint64_t xb = double_to_bits(x);
   const int ex = (int)((xb >> 52) & 0x7FF);
   if (ex == 0 || ex == 0x7FF || (xb >> 63)) {

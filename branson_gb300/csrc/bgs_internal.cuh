@@ -162,7 +162,14 @@ __device__ __forceinline__ unsigned long long rotl64(unsigned long long x, int r
   return (x << r) | (x >> (64 - r));
 }
 
+#ifndef BGS_TF_NOINLINE
+#define BGS_TF_NOINLINE 0
+#endif
+#if BGS_TF_NOINLINE
+static __device__ __noinline__ unsigned long long threefry2x64_20_w0(unsigned long long c0,
+#else
 __device__ __forceinline__ unsigned long long threefry2x64_20_w0(unsigned long long c0,
+#endif
                                                                  unsigned long long c1,
                                                                  unsigned long long k0) {
   const unsigned long long k2 = 0x1BD11BDAA9FC1A22ULL ^ k0;  // k1 = 0

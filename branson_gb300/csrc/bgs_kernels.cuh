@@ -119,10 +119,11 @@ void launch_event_init(const EventState &es, DeviceDiag *d, cudaStream_t s);
 void launch_event_round(const MeshDev &m, const CellsDev &c, const Bank &b, DeviceDiag *d, uint32_t seed,
                         const EventState &es, bool first, int n_sm, cudaStream_t s);
 
-// problem of work item w: the last p with item_off[p] <= w (n problems)
+// problem of work item w: the last p with item_off[p] <= w (n problems),
+// searched in [lo, n) (item_off[lo] <= w)
 __device__ __forceinline__ uint32_t problem_of(const unsigned long long *item_off, uint32_t n,
-                                               unsigned long long w) {
-  uint32_t lo = 0, hi = n;
+                                               unsigned long long w, uint32_t lo = 0) {
+  uint32_t hi = n;
   while (hi - lo > 1) {
     const uint32_t mid = (lo + hi) >> 1;
     if (item_off[mid] <= w) lo = mid; else hi = mid;
