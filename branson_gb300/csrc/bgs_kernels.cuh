@@ -30,6 +30,7 @@ __device__ __forceinline__ double cell_volume(const double n[6]) {
 // non-finite and out-of-range arguments take pow.
 __device__ __forceinline__ double pow_small_int_rn(double x, int n) {
   if (n == 0) return 1.0;
+  if (x == 0.0) return (n & 1) ? x : 0.0;  // pow(+-0, n > 0)
   if (!(x > 0.0) || !isfinite(x) || x > 1e60 || x < 1e-60) return pow(x, (double)n);
   double ph = x, pl = 0.0;
   for (int i = 1; i < n; ++i) {
@@ -41,6 +42,27 @@ __device__ __forceinline__ double pow_small_int_rn(double x, int n) {
     ph = s;
   }
   return ph;
+}
+
+// x^3 and x^4 as pow_small_int_rn(x, 3) and (x, 4) return them: the fourth
+// power continues the third's double-double product
+__device__ __forceinline__ void pow34_rn(double x, double &p3, double &p4) {
+  if (x == 0.0 || !(x > 0.0) || !isfinite(x) || x > 1e60 || x < 1e-60) {
+    p3 = pow_small_int_rn(x, 3);
+    p4 = pow_small_int_rn(x, 4);
+    return;
+  }
+  double ph = x, pl = 0.0;
+  for (int i = 1; i < 4; ++i) {
+    const double p = __dmul_rn(ph, x);
+    const double e = __fma_rn(ph, x, -p);
+    const double l = __fma_rn(pl, x, e);
+    const double s = __dadd_rn(p, l);
+    pl = __dsub_rn(l, __dsub_rn(s, p));
+    ph = s;
+    if (i == 2) p3 = ph;
+  }
+  p4 = ph;
 }
 
 // pow(x, c) with the small-integer exponents of the decks done exactly
@@ -67,7 +89,11 @@ __device__ __forceinline__ void set_cell_xs(const CellsDev &c, uint32_t g, doubl
   x.neg_saf = -op_a * f;
   x.inv_saf = 1.0 / (op_a * f);
   x.p_scat = op_s / ((1.0 - f) * op_a + op_s);
+#if BGS_INT_DIV_DS
   x.rb_sig = x.sig_eff > 0.0 ? fix::divisor_recip(x.sig_eff) : 0ULL;
+#else
+  x.rb_sig = 0ULL;  // only the integer-division build reads it
+#endif
   x.inv_se = recip_for_div(x.sig_eff);
   c.xs[g] = x;
   const double norm_factor = 1.0 / (op_a * (double)n_groups);

@@ -54,11 +54,13 @@ __device__ __forceinline__ void cell_energy_body(const MeshDev &m, const CellsDe
     // per-cell opacity when it supplies one (the adjoint forward)
     const double op_a = op_a_in ? op_a_in[g] : A + B * pow_deck(T, Cx);
     const double op_s = S;
-    const double f = 1.0 / (1.0 + dt * op_a * kC * (4.0 * kA * pow_small_int_rn(T, 3) / (cV * rho)));
+    double T3, T4;
+    pow34_rn(T, T3, T4);
+    const double f = 1.0 / (1.0 + dt * op_a * kC * (4.0 * kA * T3 / (cV * rho)));
     c.op_a[g] = op_a;
     c.op_s[g] = op_s;
     c.f[g] = f;
-    c.em_E[g] = rf * dt * vol * f * op_a * kA * kC * pow_small_int_rn(T, 4);
+    c.em_E[g] = rf * dt * vol * f * op_a * kA * kC * T4;
     c.ce_E[g] = (step > 1) ? 0.0 : rf * vol * kA * pow_small_int_rn(Tr, 4);
     c.so_E[g] = rf * 0.25 * kA * kC * face_area(n, c.source_face[g]) * pow_small_int_rn(Ts, 4) * dt;
     mat_E[g] = T * cV * vol * rho;
