@@ -15,6 +15,9 @@ e2e       the same metric through the drop-in call bgs_replicated_transport
           on pinned host buffers, copies in the timed region
 roofline  k_transport_history: algorithmic bytes per launch / its CUDA-event
           duration against the measured HBM copy bandwidth
+roofline_issue  the same kernel's live segments/s times ncu's thread
+          instructions per segment, against the SM issue peak (the kernel
+          is integer-ALU / FP64 bound, not HBM bound)
 cpu_baseline  the oracle (C restatement, OpenMP on every host core) on a
           bounded sample of the same deck, histories / transport time
 
@@ -150,6 +153,35 @@ class Clocks:
                         reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def issue_roofline(seg_rate, clk, tpath):
+    """Instruction-issue view of the transport kernel: live segments/s times
+    the thread instructions per segment that ncu counted on the same kernel
+    (profiles/transport_traffic.json), against the SM issue peak (4 warp
+    schedulers x 32 lanes per clock per SM) at the SM clock sampled during
+    the timed region."""
+    if not os.path.exists(tpath):
+        return None
+    with open(tpath) as fh:
+        t = json.load(fh)
+    ips = t.get("thread_instructions_per_segment")
+    if not ips:
+        return None
+    import torch
+    n_sm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = (clk or {}).get("sm_mhz") or (clk or {}).get("sm_max_mhz")
+    if not mhz:
+        return None
+    achieved = seg_rate * ips / 1e12
+    peak = 128.0 * n_sm * mhz * 1e6 / 1e12
+    fp64 = t.get("fp64_thread_instructions_per_segment")
+    return {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "T thread-instructions/s",
+            "frac": achieved / peak, "instructions_per_segment": ips,
+            "fp64_per_segment": fp64,
+            "fp64_frac": (seg_rate * fp64 / (2.0 * n_sm * mhz * 1e6)) if fp64 else None,
+            "note": "instructions per segment from ncu on the 1e6-photon case of the same deck; "
+                    "fp64_frac against 2 FP64 lanes per clock per SM"}
 
 
 def measured_peak_hbm():
@@ -291,11 +323,13 @@ def run_ours(args, rank, world, local):
         with open(tpath) as fh:
             t = json.load(fh)
         traffic = t.get("bytes_per_history", 0) * k_hist + t.get("bytes_per_cell", 0) * dk.n_cells
+    seg_rate = segs / (sum(m for m, _ in transport_ms) * 1e-3)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs",
-                "kernel": "k_transport_history", "kernel_ms": k_ms,
-                "segments_per_s": segs / (sum(m for m, _ in transport_ms) * 1e-3),
-                "note": "FP64-issue bound: the HBM fraction is small by construction"}
+                "kernel": "k_transport_history", "kernel_ms": k_ms, "segments_per_s": seg_rate,
+                "note": "integer-ALU / FP64-issue bound: the HBM fraction is small by construction; "
+                        "see roofline_issue"}
+    roofline_issue = issue_roofline(seg_rate, clk, tpath)
 
     # end to end through the drop-in call on pinned host buffers
     e2e = None
@@ -321,6 +355,7 @@ def run_ours(args, rank, world, local):
                 "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": dict(cfg, parallelism=f"replicas{world}"), "roofline": roofline,
+                "roofline_issue": roofline_issue,
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
                 "segments_per_s": segs / elapsed * world, "histories_per_step": hist / args.steps,
                 "tuning": tuning, "adjoint": adjoint, "batched": batched}

@@ -99,12 +99,12 @@ __global__ void __launch_bounds__(kAdjThreads, BGS_ADJ_MIN_BLOCKS)
           L.idx = i;
           L.px = t.px[i]; L.py = t.py[i]; L.pz = t.pz[i];
           L.dx = t.dx[i]; L.dy = t.dy[i]; L.dz = t.dz[i];
-          L.E = t.E[i]; L.E0 = t.E0[i]; L.life = t.life[i];
+          L.E = t.E[i]; L.life = t.life[i];
           L.cell = t.cell[i]; L.group = t.group[i];
           L.rng.stream = t.stream[i]; L.rng.ctr = t.ctr[i]; L.rng.hi = P.seed_hi;
           L.segs = 0;
           L.thr_abs = 0.0;
-          L.kill_thr = kCutoff * L.E0;
+          set_birth(L, t.E0[i]);
           direction_recips(L);
           xs_p = P.xs;
           ac_p = P.cell;
@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(kAdjThreads, BGS_ADJ_MIN_BLOCKS)
     const AdjCell ac = ac_p[L.cell];
     uint32_t surface_cross;
     SegInfo info;
-    const int ev = segment_advance(xs, L, surface_cross, flags, &info);
+    const int ev = segment_advance(probs[p].m, probs[p].t.E0, xs, L, surface_cross, flags, &info);
     {
       const double s = info.collided ? ac.inv_se - info.d : -info.d;
       const double gs = ac.g2 * s;

@@ -69,6 +69,10 @@ __global__ void __launch_bounds__(kItemThreads) k_batch_items(const ProblemView 
   }
 }
 
+// the batched kernel keeps the face planes ahead in registers: its mesh
+// planes sit behind the problem's view, one more dependent load per segment
+constexpr bool kBatchFaces = true;
+
 #ifndef BGS_BATCH_MIN_BLOCKS
 #define BGS_BATCH_MIN_BLOCKS 6
 #endif
@@ -108,16 +112,16 @@ __global__ void __launch_bounds__(kTransportThreads, BGS_BATCH_MIN_BLOCKS)
           L.idx = i;
           L.px = b.px[i]; L.py = b.py[i]; L.pz = b.pz[i];
           L.dx = b.dx[i]; L.dy = b.dy[i]; L.dz = b.dz[i];
-          L.E = b.E[i]; L.E0 = b.E0[i]; L.life = b.life[i];
+          L.E = b.E[i]; L.life = b.life[i];
           L.cell = b.cell[i]; L.group = b.group[i];
           L.rng.stream = b.stream[i]; L.rng.ctr = b.ctr[i]; L.rng.hi = P.seed_hi;
           L.segs = 0;
           L.thr_abs = 0.0;
-          L.kill_thr = kCutoff * L.E0;
+          set_birth(L, b.E0[i]);
           direction_recips(L);
           xs_p = P.c.xs;
           if (L.cell < P.m.n_cells) {
-            locate(P.m, L);
+            locate<kBatchFaces>(P.m, L);
             active = true;
           } else {
             atomicOr(&P.d->flags, (uint32_t)FLAG_BAD_CELL);
@@ -139,9 +143,9 @@ __global__ void __launch_bounds__(kTransportThreads, BGS_BATCH_MIN_BLOCKS)
     if (active) {
       const CellXS xs = xs_p[L.cell];
       uint32_t surface_cross;
-      const int ev = segment_advance(xs, L, surface_cross, flags);
+      const int ev = segment_advance<kBatchFaces>(probs[p].m, probs[p].from.E0, xs, L, surface_cross, flags);
       if (ev == SEG_SCATTER) {
-        scatter_update(probs[p].m, probs[p].c, xs, L);
+        scatter_update<kBatchFaces>(probs[p].m, probs[p].c, xs, L);
       } else {
         const MeshDev &m = probs[p].m;
         int bc = ELEMENT;
@@ -159,9 +163,9 @@ __global__ void __launch_bounds__(kTransportThreads, BGS_BATCH_MIN_BLOCKS)
           ended = true;
         } else if (bc == ELEMENT) {
           L.thr_abs = 0.0;
-          enter_neighbour(m, L, surface_cross);
+          enter_neighbour<kBatchFaces>(m, L, surface_cross);
         } else {
-          reflect(m, L, surface_cross);
+          reflect<kBatchFaces>(m, L, surface_cross);
         }
       }
     }

@@ -34,11 +34,11 @@ __device__ __forceinline__ void load_lane(const MeshDev &m, const Bank &b, const
   L.idx = p;
   L.px = b.px[p]; L.py = b.py[p]; L.pz = b.pz[p];
   L.dx = b.dx[p]; L.dy = b.dy[p]; L.dz = b.dz[p];
-  L.E = b.E[p]; L.E0 = b.E0[p]; L.life = b.life[p];
+  L.E = b.E[p]; L.life = b.life[p];
   L.cell = b.cell[p]; L.group = b.group[p];
   L.rng.stream = b.stream[p]; L.rng.ctr = b.ctr[p]; L.rng.hi = seed_hi;
   L.thr_abs = first ? 0.0 : es.thr_abs[p];
-  L.kill_thr = kCutoff * L.E0;
+  set_birth(L, b.E0[p]);
   L.segs = 0;
   direction_recips(L);
   locate(m, L);
@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(kEventThreads) k_event_advance(MeshDev m, Cell
       } else {
         ++segs;
         const CellXS xs = c.xs[L.cell];
-        ev = segment_advance(xs, L, sc, flags);
+        ev = segment_advance(m, b.E0, xs, L, sc, flags);
         if (ev == SEG_KILLED || ev == SEG_CENSUS) {
           flush = true;
           fcell = L.cell;

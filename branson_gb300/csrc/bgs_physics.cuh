@@ -22,7 +22,7 @@ constexpr int kTransportThreads = 128;
 #define BGS_INT_SINCOS 1
 #endif
 #ifndef BGS_MIN_BLOCKS
-#define BGS_MIN_BLOCKS 6
+#define BGS_MIN_BLOCKS 7
 #endif
 #ifndef BGS_INT_DIV_DS
 #define BGS_INT_DIV_DS 0  // -log(u)/sigma_eff by the exact integer division (per-cell reciprocal)
@@ -35,6 +35,15 @@ constexpr int kTransportThreads = 128;
 #endif
 #ifndef BGS_APPROX_FACES
 #define BGS_APPROX_FACES 1  // order the three face distances in single precision, divide once
+#endif
+#ifndef BGS_LANE_E0
+#define BGS_LANE_E0 0  // the birth weight E0 kept in registers (else read from the bank when needed)
+#endif
+#ifndef BGS_LANE_FACES
+// the face planes ahead kept in registers (else read from the mesh per
+// segment); the default of the kFaces template argument below, which a
+// kernel may set for itself
+#define BGS_LANE_FACES 0
 #endif
 #ifndef BGS_APPROX_CVT_HW
 #define BGS_APPROX_CVT_HW 0  // single-precision images by the conversion instruction (else by bits)
@@ -88,10 +97,13 @@ __device__ __forceinline__ void seg_sincos(double phi, double *s, double *c) {
 }
 
 struct Lane {
-  double px, py, pz, dx, dy, dz, E, E0, life;
+  double px, py, pz, dx, dy, dz, E, life;
+#if BGS_LANE_E0
+  double E0;
+#endif
   double kill_thr;  // RN(0.01 * E0): the cutoff test runs against it in integer ulps
   DivRecip rbx, rby, rbz;  // divisor reciprocals of the direction cosines
-  double fx, fy, fz;  // the current cell's face planes ahead along x, y, z
+  double fx, fy, fz;  // the current cell's face planes ahead along x, y, z (kFaces)
   double thr_abs;   // absorbed energy of the current cell visit
   double thr_trk;   // the visit's track tally, set by a cutoff kill (visit_track)
   unsigned long long idx;
@@ -102,10 +114,21 @@ struct Lane {
 // the node planes the photon moves toward along each axis: the upper one
 // for a positive direction cosine, else the lower one (the faces
 // get_distance_to_boundary measures to, cell.h:117-132)
+template <bool kFaces = BGS_LANE_FACES>
 __device__ __forceinline__ void load_faces(const MeshDev &m, Lane &L) {
-  L.fx = m.x[L.ci + ((__double_as_longlong(L.dx) > 0) ? 1u : 0u)];
-  L.fy = m.y[L.cj + ((__double_as_longlong(L.dy) > 0) ? 1u : 0u)];
-  L.fz = m.z[L.ck + ((__double_as_longlong(L.dz) > 0) ? 1u : 0u)];
+  if constexpr (kFaces) {
+    L.fx = m.x[L.ci + ((__double_as_longlong(L.dx) > 0) ? 1u : 0u)];
+    L.fy = m.y[L.cj + ((__double_as_longlong(L.dy) > 0) ? 1u : 0u)];
+    L.fz = m.z[L.ck + ((__double_as_longlong(L.dz) > 0) ? 1u : 0u)];
+  }
+}
+
+// a history's birth weight: E0 and the cutoff threshold RN(0.01 E0)
+__device__ __forceinline__ void set_birth(Lane &L, double E0) {
+#if BGS_LANE_E0
+  L.E0 = E0;
+#endif
+  L.kill_thr = kCutoff * E0;
 }
 
 __device__ __forceinline__ void flush_tally(const CellsDev &c, const DeviceDiag *d, uint32_t cell,
@@ -310,8 +333,10 @@ struct SegInfo {
 // faces and to census, implicit-capture decay and track tally, the move, and
 // the cutoff test (history_based_transport.h:56-91).  On SEG_KILLED the
 // remaining energy has been added to the cell's absorbed energy, as upstream.
-__device__ __forceinline__ int segment_advance(const CellXS &xs, Lane &L, uint32_t &surface_cross,
-                                               uint32_t &flags, SegInfo *info = nullptr) {
+template <bool kFaces = BGS_LANE_FACES>
+__device__ __forceinline__ int segment_advance(const MeshDev &m, const double *E0s, const CellXS &xs, Lane &L,
+                                               uint32_t &surface_cross, uint32_t &flags,
+                                               SegInfo *info = nullptr) {
   ++L.segs;
   const bool scatters = f64_positive(xs.sig_eff);
 #if BGS_INT_DIV_DS
@@ -333,9 +358,16 @@ __device__ __forceinline__ int segment_advance(const CellXS &xs, Lane &L, uint32
   long long k_boundary = f64_key(1.0e16);
   surface_cross = 0;
   const bool posx = f64_positive(L.dx), posy = f64_positive(L.dy), posz = f64_positive(L.dz);
-  const double ax = L.fx - L.px;
-  const double ay = L.fy - L.py;
-  const double az = L.fz - L.pz;
+  double ax, ay, az;
+  if constexpr (kFaces) {
+    ax = L.fx - L.px;
+    ay = L.fy - L.py;
+    az = L.fz - L.pz;
+  } else {
+    ax = m.x[L.ci + (posx ? 1u : 0u)] - L.px;
+    ay = m.y[L.cj + (posy ? 1u : 0u)] - L.py;
+    az = m.z[L.ck + (posz ? 1u : 0u)] - L.pz;
+  }
   bool decided = false;
 #if BGS_APPROX_FACES
   decided = approx_faces(ax, ay, az, L, posx, posy, posz, dist_to_boundary, k_boundary, surface_cross);
@@ -379,7 +411,12 @@ __device__ __forceinline__ int segment_advance(const CellXS &xs, Lane &L, uint32
   // closer than that the exact quotient settles it
   const long long k_e = f64_key(L.E), k_thr = f64_key(L.kill_thr);
   bool killed = k_e < k_thr;
+#if BGS_LANE_E0
+  (void)E0s;
   if (k_e - k_thr <= 4 && k_thr - k_e <= 4) killed = L.E / L.E0 < kCutoff;
+#else
+  if (k_e - k_thr <= 4 && k_thr - k_e <= 4) killed = L.E / E0s[L.idx] < kCutoff;
+#endif
   if (killed || L.segs >= kMaxSegmentsPerHistory) {
     if (!killed) flags |= FLAG_SEGMENT_LIMIT;
     L.thr_trk = L.thr_abs * xs.inv_saf;  // the visit's track tally, before the kill deposit
@@ -394,6 +431,7 @@ __device__ __forceinline__ int segment_advance(const CellXS &xs, Lane &L, uint32
 // Effective scatter (history_based_transport.h:96-99): isotropic new
 // direction (get_uniform_angle, sampling_functions.h:57-70) and, unless
 // physical scattering wins, a resampled group.
+template <bool kFaces = BGS_LANE_FACES>
 __device__ __forceinline__ void scatter_update(const MeshDev &m, const CellsDev &c, const CellXS &xs,
                                                Lane &L) {
   const double mu = mu_from_m53(L.rng.next_m53());
@@ -405,7 +443,7 @@ __device__ __forceinline__ void scatter_update(const MeshDev &m, const CellsDev 
   L.dy = sin_theta * sp;
   L.dz = mu;
   direction_recips(L);
-  load_faces(m, L);
+  load_faces<kFaces>(m, L);
   // effective-scatter test and group resample (history_based_transport.h:97-98):
   // with sigma_s = 0 the test u > 0 always passes, and with one group the
   // walk always ends in group 0, so those draws only advance the counter
@@ -435,14 +473,15 @@ __device__ __forceinline__ int face_bc(const MeshDev &m, const Lane &L, uint32_t
 
 // ELEMENT crossing: the photon enters the neighbour (cell.h:110-112); only
 // the crossed axis gets a new face ahead
+template <bool kFaces = BGS_LANE_FACES>
 __device__ __forceinline__ void enter_neighbour(const MeshDev &m, Lane &L, uint32_t surface_cross) {
   switch (surface_cross) {
-    case 0: --L.ci; L.cell -= 1; L.fx = m.x[L.ci]; break;
-    case 1: ++L.ci; L.cell += 1; L.fx = m.x[L.ci + 1]; break;
-    case 2: --L.cj; L.cell -= m.ngx; L.fy = m.y[L.cj]; break;
-    case 3: ++L.cj; L.cell += m.ngx; L.fy = m.y[L.cj + 1]; break;
-    case 4: --L.ck; L.cell -= m.ngx * m.ngy; L.fz = m.z[L.ck]; break;
-    default: ++L.ck; L.cell += m.ngx * m.ngy; L.fz = m.z[L.ck + 1]; break;
+    case 0: --L.ci; L.cell -= 1; if constexpr (kFaces) L.fx = m.x[L.ci]; break;
+    case 1: ++L.ci; L.cell += 1; if constexpr (kFaces) L.fx = m.x[L.ci + 1]; break;
+    case 2: --L.cj; L.cell -= m.ngx; if constexpr (kFaces) L.fy = m.y[L.cj]; break;
+    case 3: ++L.cj; L.cell += m.ngx; if constexpr (kFaces) L.fy = m.y[L.cj + 1]; break;
+    case 4: --L.ck; L.cell -= m.ngx * m.ngy; if constexpr (kFaces) L.fz = m.z[L.ck]; break;
+    default: ++L.ck; L.cell += m.ngx * m.ngy; if constexpr (kFaces) L.fz = m.z[L.ck + 1]; break;
   }
 }
 
@@ -450,34 +489,36 @@ __device__ __forceinline__ void enter_neighbour(const MeshDev &m, Lane &L, uint3
 // and the face ahead on that axis becomes the opposite plane of the cell.
 // An integer divisor reciprocal depends only on the magnitude; RN(1/-b) =
 // -RN(1/b) exactly.
+template <bool kFaces = BGS_LANE_FACES>
 __device__ __forceinline__ void reflect(const MeshDev &m, Lane &L, uint32_t surface_cross) {
   if (surface_cross < 2) {
     L.dx = -L.dx;
 #if !BGS_INT_DIV
     L.rbx = -L.rbx;
 #endif
-    L.fx = m.x[L.ci + ((__double_as_longlong(L.dx) > 0) ? 1u : 0u)];
+    if constexpr (kFaces) L.fx = m.x[L.ci + ((__double_as_longlong(L.dx) > 0) ? 1u : 0u)];
   } else if (surface_cross < 4) {
     L.dy = -L.dy;
 #if !BGS_INT_DIV
     L.rby = -L.rby;
 #endif
-    L.fy = m.y[L.cj + ((__double_as_longlong(L.dy) > 0) ? 1u : 0u)];
+    if constexpr (kFaces) L.fy = m.y[L.cj + ((__double_as_longlong(L.dy) > 0) ? 1u : 0u)];
   } else {
     L.dz = -L.dz;
 #if !BGS_INT_DIV
     L.rbz = -L.rbz;
 #endif
-    L.fz = m.z[L.ck + ((__double_as_longlong(L.dz) > 0) ? 1u : 0u)];
+    if constexpr (kFaces) L.fz = m.z[L.ck + ((__double_as_longlong(L.dz) > 0) ? 1u : 0u)];
   }
 }
 
 // cell coordinates and the faces ahead from the global cell index
+template <bool kFaces = BGS_LANE_FACES>
 __device__ __forceinline__ void locate(const MeshDev &m, Lane &L) {
   L.ci = L.cell % m.ngx;
   L.cj = (L.cell / m.ngx) % m.ngy;
   L.ck = L.cell / (m.ngx * m.ngy);
-  load_faces(m, L);
+  load_faces<kFaces>(m, L);
 }
 
 }  // namespace bgs

@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
           L.idx = i;
           L.px = b.px[i]; L.py = b.py[i]; L.pz = b.pz[i];
           L.dx = b.dx[i]; L.dy = b.dy[i]; L.dz = b.dz[i];
-          L.E = b.E[i]; L.E0 = b.E0[i]; L.life = b.life[i];
+          L.E = b.E[i]; L.life = b.life[i];
           L.cell = b.cell[i]; L.group = b.group[i];
           L.rng.stream = b.stream[i]; L.rng.ctr = b.ctr[i]; L.rng.hi = seed_hi;
           L.segs = 0;
@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
           } else {
             L.thr_abs = 0.0;
           }
-          L.kill_thr = kCutoff * L.E0;
+          set_birth(L, b.E0[i]);
           direction_recips(L);
           if (L.cell < m.n_cells) {
             locate(m, L);
@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
       ++seg_total;
       const CellXS xs = c.xs[L.cell];
       uint32_t surface_cross;
-      const int ev = segment_advance(xs, L, surface_cross, flags);
+      const int ev = segment_advance(m, b.E0, xs, L, surface_cross, flags);
       if (ev == SEG_SCATTER) {
         scatter_update(m, c, xs, L);
       } else {
