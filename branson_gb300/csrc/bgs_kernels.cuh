@@ -88,7 +88,9 @@ __device__ __forceinline__ void set_cell_xs(const CellsDev &c, uint32_t g, doubl
   x.sig_eff = (1.0 - f) * op_a + op_s;
   x.neg_saf = -op_a * f;
   x.inv_saf = 1.0 / (op_a * f);
-  x.p_scat = op_s / ((1.0 - f) * op_a + op_s);
+  // op_s / sigma_eff; a zero op_s over a positive finite sigma_eff is op_s itself
+  x.p_scat = (op_s == 0.0 && x.sig_eff > 0.0 && x.sig_eff < 1.7976931348623157e308) ? op_s
+                                                                                   : op_s / x.sig_eff;
 #if BGS_INT_DIV_DS
   x.rb_sig = x.sig_eff > 0.0 ? fix::divisor_recip(x.sig_eff) : 0ULL;
 #else
@@ -96,8 +98,13 @@ __device__ __forceinline__ void set_cell_xs(const CellsDev &c, uint32_t g, doubl
 #endif
   x.inv_se = recip_for_div(x.sig_eff);
   c.xs[g] = x;
-  const double norm_factor = 1.0 / (op_a * (double)n_groups);
-  c.group_v[g] = op_a * norm_factor;
+  // read only by the multigroup resample (sample_group)
+  if (n_groups > 1) {
+    const double norm_factor = 1.0 / (op_a * (double)n_groups);
+    c.group_v[g] = op_a * norm_factor;
+  } else {
+    c.group_v[g] = 1.0;
+  }
 }
 
 // ---------------------------------------------------------------- launchers

@@ -141,33 +141,39 @@ __global__ void k_energy_finish(const double *part, uint32_t n_parts, DeviceDiag
 }
 
 // could int(n_user*E/total_serial) differ from int(n_user*E/total_tree)?
-__device__ __forceinline__ bool count_ambiguous(unsigned long long n_user, double E, double total,
-                                                double window) {
-  if (!(E > 0.0)) return false;
+// photons_for(n_user, E, total) from one quotient, and whether the count
+// could differ under the serial sum: q's window of the total's error bound
+// holds an integer boundary (counts 0 and 1 both become one photon)
+__device__ __forceinline__ uint32_t count_checked(unsigned long long n_user, double E, double total, double window,
+                                                  bool &ambiguous) {
+  if (!(E > 0.0)) return 0u;
   const double q = (double)n_user * E / total;
   const double lo = q - q * window, hi = q + q * window;
-  if (hi < 2.0) return false;  // counts 0 and 1 both become one photon
-  return floor(lo) != floor(hi);
+  if (!(hi < 2.0) && floor(lo) != floor(hi)) ambiguous = true;
+  const uint32_t t = (uint32_t)(int)q;
+  return t == 0u ? 1u : t;
 }
 
-__device__ __forceinline__ void energy_check_body(const MeshDev &m, const CellsDev &c, DeviceDiag *d,
+// counts from the tree total, flagging the step when any could differ
+__device__ __forceinline__ void counts_check_body(const MeshDev &m, const CellsDev &c, DeviceDiag *d,
                                                   unsigned long long n_user, uint32_t step, uint32_t bx,
                                                   uint32_t nbx) {
   const double total = d->total_photon_E;
   // |serial - exact| <= (n-1) u sum, |tree - exact| <= (log2 n + 1) u sum,
   // plus the rounding of n*E/total: a window of (n + 64) u, doubled
   const double window = 2.0 * ((double)m.n_cells + 64.0) * 1.1102230246251565e-16;
+  bool amb = false;
   for (uint32_t g = bx * blockDim.x + threadIdx.x; g < m.n_cells; g += nbx * blockDim.x) {
-    const bool amb = count_ambiguous(n_user, c.em_E[g], total, window) ||
-                     count_ambiguous(n_user, c.so_E[g], total, window) ||
-                     (step == 1 && count_ambiguous(n_user, c.ce_E[g], total, window));
-    if (amb) d->serial_needed = 1;
+    c.n_em[g] = count_checked(n_user, c.em_E[g], total, window, amb);
+    c.n_so[g] = count_checked(n_user, c.so_E[g], total, window, amb);
+    c.n_ce[g] = step == 1 ? count_checked(n_user, c.ce_E[g], total, window, amb) : 0u;
   }
+  if (amb) d->serial_needed = 1;
 }
 
-__global__ void k_energy_check(MeshDev m, CellsDev c, DeviceDiag *d, unsigned long long n_user,
+__global__ void k_counts_check(MeshDev m, CellsDev c, DeviceDiag *d, unsigned long long n_user,
                                uint32_t step) {
-  energy_check_body(m, c, d, n_user, step, blockIdx.x, gridDim.x);
+  counts_check_body(m, c, d, n_user, step, blockIdx.x, gridDim.x);
 }
 
 // the upstream serial sum, run only when a count is ambiguous; one block
@@ -193,9 +199,11 @@ __device__ __forceinline__ void serial_total_body(const MeshDev &m, const CellsD
 
 __global__ void k_serial_total(MeshDev m, CellsDev c, DeviceDiag *d) { serial_total_body(m, c, d); }
 
-// photons per cell for emission, boundary source and (step 1) initial census
-__device__ __forceinline__ void counts_body(const MeshDev &m, const CellsDev &c, const DeviceDiag *d,
-                                            unsigned long long n_user, uint32_t step, uint32_t bx, uint32_t nbx) {
+// photons per cell for emission, boundary source and (step 1) initial
+// census from the serial total, when the checked counts were ambiguous
+__device__ __forceinline__ void recount_body(const MeshDev &m, const CellsDev &c, const DeviceDiag *d,
+                                             unsigned long long n_user, uint32_t step, uint32_t bx, uint32_t nbx) {
+  if (!d->serial_needed) return;
   const double total = d->total_photon_E;
   for (uint32_t g = bx * blockDim.x + threadIdx.x; g < m.n_cells; g += nbx * blockDim.x) {
     c.n_em[g] = photons_for(n_user, c.em_E[g], total);
@@ -204,9 +212,9 @@ __device__ __forceinline__ void counts_body(const MeshDev &m, const CellsDev &c,
   }
 }
 
-__global__ void k_counts(MeshDev m, CellsDev c, const DeviceDiag *d, unsigned long long n_user,
-                         uint32_t step) {
-  counts_body(m, c, d, n_user, step, blockIdx.x, gridDim.x);
+__global__ void k_recount(MeshDev m, CellsDev c, const DeviceDiag *d, unsigned long long n_user,
+                          uint32_t step) {
+  recount_body(m, c, d, n_user, step, blockIdx.x, gridDim.x);
 }
 
 // counts supplied by the caller (frozen across perturbed runs) must give every
@@ -509,7 +517,8 @@ __device__ __forceinline__ void update_temperature_body(const MeshDev &m, const 
       const double cV = r[0], rho = r[1];
       const double T = c.T_e[g];
       const double T_new = T + (abs_in[g] - c.em_E[g]) / (cV * vol * rho);
-      c.T_r_diag[g] = sqrt(sqrt(track_in[g] / (vol * dt * kA * kC)));  // x^(1/4) (mesh.h:358)
+      // x^(1/4) (mesh.h:358), square roots on the integer pipe (bit-identical)
+      c.T_r_diag[g] = fix::sqrt_rn(fix::sqrt_rn(track_in[g] / (vol * dt * kA * kC)));
       c.T_e[g] = T_new;
       matE = T_new * cV * vol * rho;
     }
@@ -558,9 +567,9 @@ void launch_cell_energy(const MeshDev &m, const CellsDev &c, uint32_t step, doub
   k_cell_energy<<<blocks, 256, 0, s>>>(m, c, step, dt, mat_E, op_a_in);
   k_energy_partials<<<parts, kSumThreads, 0, s>>>(m, c, mat_E, part);
   k_energy_finish<<<1, 32, 0, s>>>(part, parts, d);
-  k_energy_check<<<blocks, 256, 0, s>>>(m, c, d, n_user, step);
+  k_counts_check<<<blocks, 256, 0, s>>>(m, c, d, n_user, step);
   k_serial_total<<<1, 256, 0, s>>>(m, c, d);
-  k_counts<<<blocks, 256, 0, s>>>(m, c, d, n_user, step);
+  k_recount<<<blocks, 256, 0, s>>>(m, c, d, n_user, step);
 }
 
 void launch_cell_xs(const MeshDev &m, const CellsDev &c, cudaStream_t s) {
@@ -644,17 +653,17 @@ __global__ void k_b_energy_finish(const ProblemView *v) {
   const ProblemView &P = v[blockIdx.y];
   energy_finish_body(P.energy_part, energy_parts(P.m.n_cells), P.d);
 }
-__global__ void __launch_bounds__(256) k_b_energy_check(const ProblemView *v) {
+__global__ void __launch_bounds__(256) k_b_counts_check(const ProblemView *v) {
   const ProblemView &P = v[blockIdx.y];
-  energy_check_body(P.m, P.c, P.d, P.n_user, P.step, blockIdx.x, gridDim.x);
+  counts_check_body(P.m, P.c, P.d, P.n_user, P.step, blockIdx.x, gridDim.x);
 }
 __global__ void __launch_bounds__(256) k_b_serial_total(const ProblemView *v) {
   const ProblemView &P = v[blockIdx.y];
   serial_total_body(P.m, P.c, P.d);
 }
-__global__ void __launch_bounds__(256) k_b_counts(const ProblemView *v) {
+__global__ void __launch_bounds__(256) k_b_recount(const ProblemView *v) {
   const ProblemView &P = v[blockIdx.y];
-  counts_body(P.m, P.c, P.d, P.n_user, P.step, blockIdx.x, gridDim.x);
+  recount_body(P.m, P.c, P.d, P.n_user, P.step, blockIdx.x, gridDim.x);
 }
 // which: 0 = emission + source counts into off_new, 1 = census counts into off_ce
 __global__ void __launch_bounds__(kScanThreads) k_b_scan_counts(const ProblemView *v, int which) {
@@ -722,9 +731,9 @@ void launch_batch_energy(const ProblemView *v, const BatchGrid &g, cudaStream_t 
   k_b_cell_energy<<<dim3(g.cells, g.n), 256, 0, s>>>(v);
   k_b_energy_partials<<<dim3(g.cells, g.n), kSumThreads, 0, s>>>(v);
   k_b_energy_finish<<<dim3(1, g.n), 32, 0, s>>>(v);
-  k_b_energy_check<<<dim3(g.cells, g.n), 256, 0, s>>>(v);
+  k_b_counts_check<<<dim3(g.cells, g.n), 256, 0, s>>>(v);
   k_b_serial_total<<<dim3(1, g.n), 256, 0, s>>>(v);
-  k_b_counts<<<dim3(g.cells, g.n), 256, 0, s>>>(v);
+  k_b_recount<<<dim3(g.cells, g.n), 256, 0, s>>>(v);
   for (int which = 0; which < 2; ++which) {
     k_b_scan_counts<<<dim3(g.cell_tiles, g.n), kScanThreads, 0, s>>>(v, which);
     k_b_scan_tiles<<<dim3(1, g.n), 1024, 0, s>>>(v, which);
