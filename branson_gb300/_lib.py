@@ -94,6 +94,8 @@ SIGNATURES = (
     ("bgs_step", C.c_int, [C.c_void_p, C.POINTER(StepParams), C.POINTER(TransportDiag)]),
     ("bgs_synchronize", C.c_int, [C.c_void_p]),
     ("bgs_bank_size", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
+    ("bgs_comb_census", C.c_int, [C.c_void_p, C.c_int64, C.c_uint32, C.c_uint64, C.POINTER(C.c_uint64),
+                                  C.POINTER(C.c_uint64)]),
     ("bgs_get_photons", C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.POINTER(PhotonsHost)]),
     ("bgs_set_photons", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(PhotonsHost)]),
     ("bgs_replicated_transport", C.c_int,

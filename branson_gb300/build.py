@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libbranson_gb300.so")
 SOURCES = ("bgs_api.cu", "bgs_mesh.cu", "bgs_source.cu", "bgs_transport.cu", "bgs_event.cu", "bgs_noalloc.cu",
-           "bgs_adjoint.cu", "bgs_adjoint_api.cu", "bgs_batch.cu", "bgs_batch_api.cu")
+           "bgs_adjoint.cu", "bgs_adjoint_api.cu", "bgs_batch.cu", "bgs_batch_api.cu", "bgs_comb.cu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-fvisibility=hidden", "--expt-relaxed-constexpr",

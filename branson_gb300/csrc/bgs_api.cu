@@ -182,6 +182,7 @@ int bgs_destroy(bgs_context *ctx) {
   free_list(ctx->bank_allocs);
   free_list(ctx->event_allocs);
   free_list(ctx->adj_allocs);
+  free_list(ctx->comb_allocs);
   if (ctx->h_counter) cudaFreeHost(ctx->h_counter);
   if (ctx->d_diag) cudaFree(ctx->d_diag);
   if (ctx->h_diag) cudaFreeHost(ctx->h_diag);

@@ -64,6 +64,15 @@ struct bgs_context {
   std::vector<unsigned long long> h_adj_item_off;
   unsigned long long mesh_generation = 0;  // bumped by every bgs_set_mesh
 
+  // census comb (allocated on first use): radix-sort buffers, cell ranges
+  std::vector<void *> comb_allocs;
+  uint32_t *comb_keys = nullptr, *comb_pos = nullptr;  // 2n each: sort input, output
+  uint32_t *comb_first = nullptr;                      // 2 n_cells: first, last sorted slot
+  double *comb_scalars = nullptr;                      // list energy, comb energy
+  uint8_t *comb_temp = nullptr;
+  uint32_t comb_cap = 0, comb_cells_cap = 0;
+  size_t comb_temp_bytes = 0;
+
   DeviceDiag *d_diag = nullptr;
   DeviceDiag *h_diag = nullptr;  // pinned
   TransportLaunch tshape{};

@@ -13,7 +13,7 @@ from __future__ import annotations
 
 import ctypes as C
 from dataclasses import dataclass
-from typing import Dict, Optional
+from typing import Dict, Optional, Tuple
 
 import numpy as np
 
@@ -181,6 +181,20 @@ class ReplicatedIMC:
         s = out.struct()
         self._check(self.lib.bgs_get_photons(self.ctx, offset, count, C.byref(s)), "bgs_get_photons")
         return out
+
+    def comb_census(self, max_census_photons: int, stream: int, counter: int = 0,
+                    seed: Optional[int] = None) -> Tuple[int, int]:
+        """comb_photons (census_functions.h:48-93) on the census the last
+        transport left in the bank, with RNG(seed, stream) from ``counter``
+        (the deck's seed by default).  Returns (census photons kept, the RNG
+        counter after the comb's draws); the next step starts from the kept
+        census."""
+        seed = self.deck.seed if seed is None else seed
+        ctr = C.c_uint64(counter)
+        n = C.c_uint64()
+        self._check(self.lib.bgs_comb_census(self.ctx, int(max_census_photons), seed, stream, C.byref(ctr),
+                                             C.byref(n)), "bgs_comb_census")
+        return int(n.value), int(ctr.value)
 
     def set_photons(self, ph: PhotonArrays) -> None:
         s = ph.struct()

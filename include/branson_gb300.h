@@ -29,6 +29,7 @@
  *                                (replicated_transport.h:33-38) with host
  *                                photon buffers: the drop-in the C++ shim in
  *                                branson_gb300_transport.hpp calls
+ *   bgs_comb_census              comb_photons (census_functions.h:48-93)
  */
 #ifndef BRANSON_GB300_H
 #define BRANSON_GB300_H
@@ -172,6 +173,19 @@ BGS_API int bgs_bank_size(bgs_context *ctx, uint64_t *n);
 /* Copy photons [offset, offset+count) of the current bank out / in. */
 BGS_API int bgs_get_photons(bgs_context *ctx, uint64_t offset, uint64_t count, const bgs_photons_host *out);
 BGS_API int bgs_set_photons(bgs_context *ctx, uint64_t count, const bgs_photons_host *in);
+
+/* Census population control: comb_photons (census_functions.h:48-93) on
+ * the census the last transport left in the bank, in bank order, with the
+ * caller's RNG(seed, stream) at *rng_counter (RNG.h:318-340): the comb
+ * energy is the census's left-to-right energy sum over max_census_photons;
+ * census photon k draws number k and survives if the draw exceeds
+ * 1 - E/comb_E or it is the last photon left in its cell; survivors take
+ * the comb energy plus an equal share of their cell's energy defect.  The
+ * survivors (in bank order) become the census the next step starts from.
+ * *rng_counter advances by one per census photon; *n_census (may be NULL)
+ * receives the survivors.  BGS_ERR_STATE unless the bank holds a census. */
+BGS_API int bgs_comb_census(bgs_context *ctx, int64_t max_census_photons, uint32_t seed, uint64_t stream,
+                            uint64_t *rng_counter, uint64_t *n_census);
 
 /* ------------------------------------------------ drop-in transport */
 /* replicated_transport<Census_T> (replicated_transport.h:33-158) on host

@@ -597,6 +597,48 @@ size_t bo_post_process(double next_dt, bo_photon *photons, size_t n, bo_photon *
   return nc;
 }
 
+/* comb_photons (census_functions.h:48-93) */
+size_t bo_comb_census(const bo_photon *photons, size_t n, uint32_t n_cells, int64_t max_census, uint32_t seed,
+                      uint64_t stream, uint64_t *counter, bo_photon *out) {
+  /* get_photon_list_E (census_functions.h:40-46); the allreduce is one rank */
+  double census_E = 0.0;
+  for (size_t k = 0; k < n; ++k) census_E += photons[k].E;
+  const double comb_E = census_E / (double)max_census;
+  uint32_t *count = calloc(n_cells ? n_cells : 1, sizeof(uint32_t));
+  double *cell_E = calloc(n_cells ? n_cells : 1, sizeof(double));
+  double *corrected = calloc(n_cells ? n_cells : 1, sizeof(double));
+  for (size_t k = 0; k < n; ++k) {
+    count[photons[k].cell]++;
+    cell_E[photons[k].cell] += photons[k].E;
+  }
+  bo_rng r;
+  rng_init(&r, seed, stream, *counter);
+  size_t m = 0;
+  for (size_t k = 0; k < n; ++k) {
+    const bo_photon p = photons[k];
+    const uint32_t cell = p.cell;
+    const double p_kill = 1.0 - p.E / comb_E;
+    const double u = rng_next(&r);
+    if (u > p_kill || count[cell] == 1) {
+      out[m] = p;
+      out[m].E = comb_E;
+      corrected[cell] += comb_E;
+      ++m;
+    } else {
+      count[cell]--;
+    }
+  }
+  for (size_t j = 0; j < m; ++j) {
+    const uint32_t cell = out[j].cell;
+    out[j].E = out[j].E + (cell_E[cell] - corrected[cell]) / (double)count[cell];
+  }
+  *counter = r.counter;
+  free(count);
+  free(cell_E);
+  free(corrected);
+  return m;
+}
+
 /* Mesh::update_temperature (mesh.h:349-362, :419-422) */
 void bo_update_temperature(const bo_mesh *m, bo_cells *c, double dt, double *abs_E,
                            double *track_E, double *total_abs_E, double *post_mat_E) {

@@ -102,6 +102,18 @@ uint64_t bo_transport(const bo_mesh *m, const bo_cells *c, uint32_t seed, bo_pho
 size_t bo_post_process(double next_dt, bo_photon *photons, size_t n, bo_photon *census_out,
                        double *census_E, double *exit_E);
 
+/* comb_photons (census_functions.h:48-93), census population control: the
+ * comb energy is the list's left-to-right energy sum over max_census; photon
+ * k of the list takes draw k of RNG(seed, stream) from *counter (one draw per
+ * photon) and survives when the draw exceeds 1 - E/comb_E or it is the only
+ * photon left in its cell; survivors take the comb energy, and then every
+ * survivor of a cell gets an equal share of the cell's energy defect.  The
+ * per-cell maps are arrays over n_cells with sums in list order, as upstream.
+ * Survivors are written in list order to out (which may alias photons);
+ * returns their number and advances *counter past the draws. */
+size_t bo_comb_census(const bo_photon *photons, size_t n, uint32_t n_cells, int64_t max_census, uint32_t seed,
+                      uint64_t stream, uint64_t *counter, bo_photon *out);
+
 /* Mesh::update_temperature (mesh.h:327-362); abs/track are zeroed. */
 void bo_update_temperature(const bo_mesh *m, bo_cells *c, double dt, double *abs_E,
                            double *track_E, double *total_abs_E, double *post_mat_E);

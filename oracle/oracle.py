@@ -100,6 +100,9 @@ def lib():
         L.bo_adjoint_replay.restype = C.c_uint64
         L.bo_adjoint_replay.argtypes = [C.POINTER(_Mesh), C.POINTER(_Cells), C.c_uint32, pp, C.c_size_t, dp,
                                         C.c_int, C.c_double, dp, C.c_int]
+        L.bo_comb_census.restype = C.c_size_t
+        L.bo_comb_census.argtypes = [pp, C.c_size_t, C.c_uint32, C.c_int64, C.c_uint32, C.c_uint64,
+                                     C.POINTER(C.c_uint64), pp]
         L.bo_adjoint_reweighted.restype = C.c_double
         L.bo_adjoint_reweighted.argtypes = [C.POINTER(_Mesh), C.POINTER(_Cells), dp, dp, C.c_uint32, pp,
                                             C.c_size_t, dp]
@@ -311,6 +314,18 @@ def adjoint_scale(w, start, op_a, op_s, f, n_segments):
     return 118 - e, bound
 
 
+def comb(census: np.ndarray, n_cells: int, max_census: int, seed: int, stream: int, counter: int = 0):
+    """comb_photons (census_functions.h:48-93) on a census list (PHOTON_DTYPE
+    records, list order) with RNG(seed, stream) from ``counter``: returns the
+    combed list and the RNG counter after its draws (bo_comb_census)."""
+    src = np.ascontiguousarray(census, dtype=PHOTON_DTYPE)
+    out = np.empty_like(src)
+    ctr = C.c_uint64(counter)
+    m = lib().bo_comb_census(src.ctypes.data, len(src), n_cells, int(max_census), seed, stream, C.byref(ctr),
+                             out.ctypes.data)
+    return out[:m].copy(), int(ctr.value)
+
+
 def read_harness_step(out_dir: str, step: int, n_cells: int) -> dict:
     """Load one step of oracle/ref_harness.cc output."""
     def rec(name):
@@ -321,12 +336,15 @@ def read_harness_step(out_dir: str, step: int, n_cells: int) -> dict:
         for line in fh:
             k, v = line.split()
             scalars[k] = float(v)
-    return {"source": rec("source"), "end": rec("end"), "census": rec("census"), "cells": cells,
-            "scalars": scalars}
+    out = {"source": rec("source"), "end": rec("end"), "census": rec("census"), "cells": cells,
+           "scalars": scalars}
+    if os.path.exists(os.path.join(out_dir, f"step{step:03d}_comb.bin")):
+        out["comb"] = rec("comb")
+    return out
 
 
 def run_reference_harness(deck, out_dir: str, n_steps: int, n_threads: int = 1, dump: bool = True,
-                          timeout: Optional[float] = None) -> str:
+                          timeout: Optional[float] = None, comb: Optional[tuple] = None) -> str:
     """Run the upstream-header harness (oracle/_ref) on ``deck``; returns stdout."""
     exe = os.path.join(REF_DIR, "ref_harness_g30" if deck.n_groups == 30 else "ref_harness_g1")
     if deck.n_groups not in (1, 30):
@@ -338,5 +356,7 @@ def run_reference_harness(deck, out_dir: str, n_steps: int, n_threads: int = 1, 
     with open(path, "w") as fh:
         fh.write(deck.to_xml())
     args = [exe, path, out_dir, str(n_steps), str(n_threads)] + ([] if dump else ["--no-dump"])
+    if comb is not None:  # (max_census_photons, stream): comb each step's census
+        args += ["--comb", str(int(comb[0])), str(int(comb[1]))]
     r = subprocess.run(args, capture_output=True, text=True, timeout=timeout, check=True)
     return r.stdout

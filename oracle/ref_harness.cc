@@ -13,6 +13,7 @@
 //   update_temperature (mesh.h:327)                  -> cells_post
 //
 // Usage: ref_harness <deck.xml> <out_dir> <n_steps> <n_threads> [--no-dump]
+//                    [--comb <max_census_photons> <stream>]
 // Output (little endian):
 //   cells.bin                 per cell: nodes[6] (f64), region_ID (u32), pad
 //   stepNNN_source.bin        photon records before transport
@@ -21,6 +22,10 @@
 //   stepNNN_cells.bin         per cell: op_a f emission_E census_E source_E
 //                             abs_E track_E T_e_new T_r  (9 x f64)
 //   stepNNN_scalars.txt       key value lines (conservation, counts, timing)
+//   stepNNN_comb.bin          (--comb) the census after comb_photons
+//                             (census_functions.h:48-93) with a fresh
+//                             RNG(seed, stream); the step itself goes on
+//                             with the uncombed census
 // Photon record (104 B): stream u64, counter u64, cell u32, group u32,
 //   source_type u32, descriptor u32, pos[3] dir[3] E E0 life_dx (9 x f64).
 
@@ -122,7 +127,19 @@ int main(int argc, char **argv) {
   const std::string out = argv[2];
   const int n_steps = std::atoi(argv[3]);
   const int n_threads = std::atoi(argv[4]);
-  const bool dump = !(argc > 5 && std::string(argv[5]) == "--no-dump");
+  bool dump = true;
+  int64_t comb_max = 0;
+  uint64_t comb_stream = 0;
+  for (int a = 5; a < argc; ++a) {
+    const std::string opt = argv[a];
+    if (opt == "--no-dump") {
+      dump = false;
+    } else if (opt == "--comb" && a + 2 < argc) {
+      comb_max = std::atoll(argv[a + 1]);
+      comb_stream = std::strtoull(argv[a + 2], nullptr, 10);
+      a += 2;
+    }
+  }
 
   MPI_Init(&argc, &argv);
   const Info mpi_info;
@@ -204,6 +221,16 @@ int main(int argc, char **argv) {
       dump_photons(step_name(out, step, "end.bin"), all_photons);
       dump_photons(step_name(out, step, "census.bin"), census_photons);
     }
+    uint64_t comb_draws = 0;
+    if (dump && comb_max > 0) {
+      std::vector<Photon> combed = census_photons;
+      RNG comb_rng(seed, comb_stream);
+      comb_photons(combed, comb_max, &comb_rng);
+      uint64_t words[4];
+      std::memcpy(words, &comb_rng, sizeof(words));
+      comb_draws = words[0];
+      dump_photons(step_name(out, step, "comb.bin"), combed);
+    }
     std::vector<double> tallies_abs(abs_E.begin(), abs_E.begin() + n_cells);
     std::vector<double> tallies_track(track_E.begin(), track_E.begin() + n_cells);
 
@@ -238,6 +265,11 @@ int main(int argc, char **argv) {
     std::fprintf(f, "census_size %llu\n", (unsigned long long)census_photons.size());
     std::fprintf(f, "post_census_E %.17g\n", get_photon_list_E(census_photons));
     std::fprintf(f, "transport_s %.9g\n", transport_s);
+    if (comb_max > 0) {
+      std::fprintf(f, "comb_max %lld\n", (long long)comb_max);
+      std::fprintf(f, "comb_stream %llu\n", (unsigned long long)comb_stream);
+      std::fprintf(f, "comb_draws %llu\n", (unsigned long long)comb_draws);
+    }
     if (dump)
       std::fclose(f);
     imc_state.print_conservation(imc_p.get_dd_mode());

@@ -17,12 +17,25 @@ pytestmark = pytest.mark.gpu
 C_LIGHT = 299.792458
 
 
+def _uniform_deck():
+    """Eight identical cells, emission only (T_r = 0, no source face), 8000
+    photons: each cell's count n*E/total sits on the integer 1000, inside the
+    error window of the tree-summed total, so the step takes the upstream
+    serial sum and recounts (source.h:225-245, mesh.h:282-287)."""
+    from branson_gb300.deck import Deck, Division, Region, VACUUM
+    return Deck(t_start=0.0, t_stop=0.03, dt_start=0.01, t_mult=1.0, dt_max=1.0, photons=8000, seed=11,
+                x_divisions=[Division(0.0, 1.0, 2)], y_divisions=[Division(0.0, 1.0, 2)],
+                z_divisions=[Division(0.0, 1.0, 2)], region_map={(0, 0, 0): 1}, bc=(VACUUM,) * 6, T_source=0.0,
+                regions=[Region(1, 0.1, 1.0, 10.0, 0.0, 0.0, 0.0, 0.5, 0.0)])
+
+
 def _decks():
     from branson_gb300 import deck as D
     return {
         "marshak": D.marshak_wave(n_cells=100, photons=20000, n_steps=3),
         "hot_zone": D.hot_zone(n_per_axis=10, photons=20000, n_steps=3),
         "hohlraum30": D.hohlraum(n_per_axis=10, photons=20000, n_steps=2, n_groups=30),
+        "uniform8": _uniform_deck(),
     }
 
 
@@ -72,7 +85,7 @@ def test_dropin_transport_matches_oracle(gpu_lib, name):
         gpu.close()
 
 
-@pytest.mark.parametrize("name", ["marshak", "hot_zone", "hohlraum30"])
+@pytest.mark.parametrize("name", ["marshak", "hot_zone", "hohlraum30", "uniform8"])
 def test_device_step_matches_oracle(gpu_lib, name):
     import oracle as O
     from branson_gb300.engine import ReplicatedIMC, arrays_to_records

@@ -66,6 +66,40 @@ def test_oracle_matches_upstream_golden(name):
         assert r.total_photon_E == pytest.approx(sc["total_photon_E"], rel=1e-15)
 
 
+def test_comb_matches_upstream_golden():
+    """comb_photons (census_functions.h:48-93) run by the upstream headers on
+    each step's census of the Marshak fixture: the oracle's restatement
+    (bo_comb_census) keeps the same photons with the same energies, bit for
+    bit on any host (only IEEE +, -, / and the Threefry words are involved),
+    and advances the comb RNG by one draw per census photon."""
+    import oracle as O
+    g = _golden("comb_marshak_g1")
+    for s in range(1, int(g["n_steps"]) + 1):
+        census, ref = g[f"s{s}_census"], g[f"s{s}_comb"]
+        got, ctr = O.comb(census, int(g["n_cells"]), int(g["comb_max"]), int(g["seed"]), int(g["comb_stream"]))
+        assert len(ref) < len(census) and len(got) == len(ref)
+        for f in ref.dtype.names:
+            np.testing.assert_array_equal(got[f], ref[f], err_msg=f"comb s{s} {f}")
+        assert ctr == int(g[f"s{s}_comb_draws"]) == len(census)
+
+
+def test_comb_keeps_the_last_photon_of_a_cell():
+    """A cell whose earlier photons are all combed away keeps its last one
+    (the count == 1 rule); per-cell energy is conserved up to the rounding of
+    the comb energy (the defect share cancels against it)."""
+    import oracle as O
+    rec = np.zeros(6, dtype=O.PHOTON_DTYPE)
+    rec["cell"] = [0, 1, 0, 1, 2, 0]
+    rec["E"] = [1e-9, 2e-9, 3e-9, 1.0, 1e-9, 2e-9]  # tiny photons, one large in cell 1
+    out, ctr = O.comb(rec, 3, 2, 7, 99)
+    assert ctr == 6
+    cells = set(int(c) for c in out["cell"])
+    assert cells == {0, 1, 2}  # every cell keeps at least one photon
+    for c in range(3):
+        np.testing.assert_allclose(out["E"][out["cell"] == c].sum(), rec["E"][rec["cell"] == c].sum(),
+                                   rtol=0.0, atol=1e-15 * rec["E"].sum())
+
+
 def test_conservation_identities():
     """Radiation and material energy balance of the step (imc_state.h:254-258)."""
     import oracle as O
