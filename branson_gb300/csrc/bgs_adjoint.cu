@@ -105,7 +105,6 @@ __global__ void __launch_bounds__(kAdjThreads, BGS_ADJ_MIN_BLOCKS)
           L.segs = 0;
           L.thr_abs = 0.0;
           set_birth(L, t.E0[i]);
-          direction_recips(L);
           xs_p = P.xs;
           ac_p = P.cell;
           prefix = 0.0; vis_a = 0.0; vis_b = 0.0;

@@ -118,7 +118,6 @@ __global__ void __launch_bounds__(kTransportThreads, BGS_BATCH_MIN_BLOCKS)
           L.segs = 0;
           L.thr_abs = 0.0;
           set_birth(L, b.E0[i]);
-          direction_recips(L);
           xs_p = P.c.xs;
           if (L.cell < P.m.n_cells) {
             locate<kBatchFaces>(P.m, L);

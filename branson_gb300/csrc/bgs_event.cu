@@ -40,7 +40,6 @@ __device__ __forceinline__ void load_lane(const MeshDev &m, const Bank &b, const
   L.thr_abs = first ? 0.0 : es.thr_abs[p];
   set_birth(L, b.E0[p]);
   L.segs = 0;
-  direction_recips(L);
   locate(m, L);
 }
 

@@ -30,10 +30,6 @@
 
 #include "bgs_fixmath_tables.h"
 
-#ifndef BGS_FIX_NOINLINE
-#define BGS_FIX_NOINLINE 0
-#endif
-
 #if defined(__CUDACC__)
 #define BGS_HD __host__ __device__ __forceinline__
 // one shared copy in device code: routines called from several places of
@@ -43,13 +39,6 @@
 #else
 #define BGS_HD inline
 #define BGS_HD_SHARED inline
-#endif
-// the per-segment routines (log, exp, sin/cos, sqrt): inlined, or one
-// out-of-line copy each
-#if BGS_FIX_NOINLINE
-#define BGS_HD_ROUTINE BGS_HD_SHARED
-#else
-#define BGS_HD_ROUTINE BGS_HD
 #endif
 
 namespace bgs {
@@ -156,7 +145,7 @@ BGS_HD_SHARED double round_u128(u128 W, int scale) {
 // -ln(u) for the RNG draw u = m * 2^-53 (u01fixedpt: m odd, 1 <= m < 2^53).
 // The result is the value -log(u) rounds to (the upstream distance to
 // collision numerator, history_based_transport.h:62-63).
-BGS_HD_ROUTINE double neg_log_u53(uint64_t m) {
+BGS_HD double neg_log_u53(uint64_t m) {
   const uint64_t n = (1ULL << 53) - m;  // v = 1 - u = n * 2^-53, exact
   if (n < (1ULL << 42)) {
     // v < 2^-11: -ln(1-v) = v (1 + v/2 + v^2/3 + v^3/4 + v^4/5 + v^5/6), V = v*2^64
@@ -197,7 +186,7 @@ BGS_HD_ROUTINE double neg_log_u53(uint64_t m) {
 // exp(-tau) for tau >= 0: the factor exp(-sigma_a*f*d) of the implicit-capture
 // weight decay (history_based_transport.h:74).  tau above 700 (result below
 // 1e-304) returns the CUDA/libm value instead of the fixed-point path.
-BGS_HD_ROUTINE double exp_neg(double tau) {
+BGS_HD double exp_neg(double tau) {
   const uint64_t tb = double_to_bits(tau);
   const int te = (int)((tb >> 52) & 0x7FF);
   if (te == 0) return 1.0;  // tau = 0 (or subnormal: exp rounds to 1)
@@ -257,7 +246,7 @@ struct SinCos {
   double s, c;
 };
 
-BGS_HD_ROUTINE SinCos sincos_phi_v(double phi) {
+BGS_HD SinCos sincos_phi_v(double phi) {
   constexpr uint64_t kS[10] = {BGS_SIN_COEF_INIT};
   constexpr uint64_t kCo[10] = {BGS_COS_COEF_INIT};
   const uint64_t pb = double_to_bits(phi);
@@ -342,10 +331,10 @@ BGS_HD void sincos_phi(double phi, double *s_out, double *c_out) {
 
 
 // ------------------------------------------------------------------------
-// Correctly rounded division and square root in integer arithmetic.  These
-// reproduce IEEE-754 round-to-nearest-even results exactly (they are checked
-// bit for bit against the hardware FP64 operations) for positive normal
-// operands and normal results; anything else goes to the FP64 operation.
+// Correctly rounded square root in integer arithmetic.  It reproduces the
+// IEEE-754 round-to-nearest-even result exactly (checked bit for bit against
+// the hardware FP64 square root) for positive normal operands; anything else
+// goes to the FP64 operation.
 
 // floor(f * 2^shift) for a positive normal float, from its bits, saturating
 // at 2^64 - 1 (no floating-point conversion instruction needed)
@@ -371,99 +360,10 @@ BGS_HD float u64_to_float_approx(uint64_t x) {  // x < 2^24, exact
 #endif
 }
 
-// floor(2^116 / M) for a 53-bit mantissa M in (2^52, 2^53): a 64-bit
-// reciprocal, from a float seed refined by two Newton steps in fixed point
-// and corrected to the exact floor.
-BGS_HD_SHARED uint64_t recip116(uint64_t M) {
-  const float mf = u64_to_float_approx(M >> 29);  // M / 2^29, 24 bits
-#if defined(__CUDA_ARCH__)
-  const float rf = __frcp_rn(mf);
-#else
-  const float rf = 1.0f / mf;
-#endif
-  uint64_t r = float_to_fixed(rf, 87);  // ~2^116/M
-  // Newton: r <- r (2 - M r / 2^116) in fixed point, twice
-#pragma unroll 1
-  for (int it = 0; it < 2; ++it) {
-    const u128 mr = (u128)M * r;
-    const u128 err = (((u128)1) << 117) - mr;  // (2 - M r/2^116) * 2^116
-    r = (uint64_t)(((u128)r * (uint64_t)(err >> 53)) >> 63);
-  }
-  // exact correction to floor(2^116/M)
-  const u128 P = ((u128)1) << 116;
-  u128 mr = (u128)M * r;
-#pragma unroll 1
-  for (int it = 0; it < 8 && mr > P; ++it) { --r; mr -= M; }
-#pragma unroll 1
-  for (int it = 0; it < 8 && P - mr >= M; ++it) { ++r; mr += M; }
-  return r;
-}
-
-// the reciprocal div_rn wants for divisor b: recip116 of its mantissa, or 0
-// when the mantissa is 2^52 (b a power of two)
-BGS_HD uint64_t divisor_recip(double b) {
-  const uint64_t M = (double_to_bits(b) & 0x000FFFFFFFFFFFFFULL) | 0x0010000000000000ULL;
-  return M == 0x0010000000000000ULL ? 0ULL : recip116(M);
-}
-
-// settle the rounding of Ma/Mb exactly: the candidate qt (53 bits) is
-// compared with the true quotient through 128-bit products; c_hi asks whether
-// the estimate may sit just below qt + 1
-BGS_HD_SHARED uint64_t div_settle(uint64_t Ma, uint64_t Mb, uint64_t qt, int s, bool next) {
-  const u128 lhs = (u128)Ma << (s + 1);
-  if (next) {
-    const uint64_t c = qt + 1;
-    const u128 mid = (u128)(2 * c + 1) * Mb;
-    return lhs > mid ? c + 1 : (lhs == mid ? ((c & 1) ? c + 1 : c) : c);
-  }
-  const u128 mid = (u128)(2 * qt + 1) * Mb;
-  const bool above = lhs > mid, tie = lhs == mid;
-  return qt + ((above || (tie && (qt & 1))) ? 1 : 0);
-}
-
-// a / b rounded to nearest even, with rb = divisor_recip(b).
-BGS_HD double div_rn(double a, double b, uint64_t rb) {
-  const uint64_t ab = double_to_bits(a), bb = double_to_bits(b);
-  const int ea = (int)((ab >> 52) & 0x7FF), eb = (int)((bb >> 52) & 0x7FF);
-  if (ea == 0 || ea == 0x7FF || eb == 0 || eb == 0x7FF) return a / b;
-  const uint64_t Ma = (ab & 0x000FFFFFFFFFFFFFULL) | 0x0010000000000000ULL;
-  const uint64_t Mb = (bb & 0x000FFFFFFFFFFFFFULL) | 0x0010000000000000ULL;
-  const uint64_t sign = ((ab ^ bb) >> 63) << 63;
-  int e = ea - eb;  // q = Ma/Mb * 2^e
-  uint64_t q;       // 53-bit result mantissa
-  if (Mb == 0x0010000000000000ULL) {
-    q = Ma;  // exact
-  } else {
-    // Q ~ Ma/Mb * 2^63 (error < 2 units), Ma/Mb in (1/2, 2)
-    const uint64_t Q = (uint64_t)(((u128)(Ma << 11) * rb) >> 64);
-    // position the quotient: if Ma >= Mb, Q in [2^63, 2^64); else [2^62, 2^63)
-    const bool big = Ma >= Mb;
-    if (!big) e -= 1;
-    const int drop = big ? 11 : 10;            // bits below the 53-bit mantissa
-    uint64_t qt = Q >> drop;                   // truncated candidate
-    const uint64_t rem = Q & ((1ULL << drop) - 1);
-    const uint64_t halfw = 1ULL << (drop - 1);
-    // decide by the exact remainder when the estimate is near a boundary:
-    // compare Ma * 2^s with (qt + 1/2) * Mb, s = 52 (big) or 53
-    if (rem + 4 >= halfw && rem <= halfw + 4) {
-      qt = div_settle(Ma, Mb, qt, big ? 52 : 53, false);
-    } else if (rem > halfw) {
-      ++qt;
-    } else if (rem + 4 >= (1ULL << drop)) {
-      qt = div_settle(Ma, Mb, qt, big ? 52 : 53, true);
-    }
-    q = qt;
-    if (q >> 53) { q >>= 1; e += 1; }
-  }
-  const int be = e + 1023;
-  if (be <= 0 || be >= 0x7FF) return a / b;
-  return bits_to_double(sign | ((uint64_t)be << 52) | (q & 0x000FFFFFFFFFFFFFULL));
-}
-
 // sqrt(x) rounded to nearest for normal x > 0: 1/sqrt by Newton in fixed
 // point from a float seed, the root w*r, then the exact floor and rounding
 // checked with 128-bit integer squares.
-BGS_HD_ROUTINE double sqrt_rn(double x) {
+BGS_HD double sqrt_rn(double x) {
   const uint64_t xb = double_to_bits(x);
   const int ex = (int)((xb >> 52) & 0x7FF);
   if (ex == 0 || ex == 0x7FF || (xb >> 63)) {

@@ -54,12 +54,8 @@ constexpr uint32_t kMaxSegmentsPerHistory = 100000000u;
 //   inv_se   = RN(1/sig_eff) for the correctly rounded division
 //              -log(u)/sig_eff by one multiply and two fma (div_recip in
 //              bgs_physics.cuh); 0 if sig_eff is 0 or out of that range
-//   rb_sig   = 64-bit reciprocal of sig_eff's mantissa for the exact integer
-//              division -log(u)/sig_eff (bgs_fixmath.cuh div_rn)
 struct __align__(16) CellXS {
-  double sig_eff, neg_saf, inv_saf, p_scat;
-  unsigned long long rb_sig;
-  double inv_se;
+  double sig_eff, neg_saf, inv_saf, p_scat, inv_se;
 };
 
 // 128-bit fixed-point tally cell: value = (hi*2^64 + lo) * 2^-scale.
@@ -162,14 +158,7 @@ __device__ __forceinline__ unsigned long long rotl64(unsigned long long x, int r
   return (x << r) | (x >> (64 - r));
 }
 
-#ifndef BGS_TF_NOINLINE
-#define BGS_TF_NOINLINE 0
-#endif
-#if BGS_TF_NOINLINE
-static __device__ __noinline__ unsigned long long threefry2x64_20_w0(unsigned long long c0,
-#else
 __device__ __forceinline__ unsigned long long threefry2x64_20_w0(unsigned long long c0,
-#endif
                                                                  unsigned long long c1,
                                                                  unsigned long long k0) {
   const unsigned long long k2 = 0x1BD11BDAA9FC1A22ULL ^ k0;  // k1 = 0

@@ -91,11 +91,6 @@ __device__ __forceinline__ void set_cell_xs(const CellsDev &c, uint32_t g, doubl
   // op_s / sigma_eff; a zero op_s over a positive finite sigma_eff is op_s itself
   x.p_scat = (op_s == 0.0 && x.sig_eff > 0.0 && x.sig_eff < 1.7976931348623157e308) ? op_s
                                                                                    : op_s / x.sig_eff;
-#if BGS_INT_DIV_DS
-  x.rb_sig = x.sig_eff > 0.0 ? fix::divisor_recip(x.sig_eff) : 0ULL;
-#else
-  x.rb_sig = 0ULL;  // only the integer-division build reads it
-#endif
   x.inv_se = recip_for_div(x.sig_eff);
   c.xs[g] = x;
   // read only by the multigroup resample (sample_group)

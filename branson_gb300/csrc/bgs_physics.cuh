@@ -9,44 +9,10 @@
 namespace bgs {
 
 constexpr int kTransportThreads = 128;
-// Build-time choices for the per-segment arithmetic (see the header comment
-// of bgs_fixmath.cuh): integer or FP64 for the divisions, the square root
-// and sin/cos, and the minimum number of resident blocks per SM.
-#ifndef BGS_INT_DIV
-#define BGS_INT_DIV 0
-#endif
-#ifndef BGS_INT_SQRT
-#define BGS_INT_SQRT 1
-#endif
-#ifndef BGS_INT_SINCOS
-#define BGS_INT_SINCOS 1
-#endif
+// Minimum resident 128-thread blocks per SM of the history kernel (its
+// register budget: 7 blocks is 72 registers)
 #ifndef BGS_MIN_BLOCKS
 #define BGS_MIN_BLOCKS 7
-#endif
-#ifndef BGS_INT_DIV_DS
-#define BGS_INT_DIV_DS 0  // -log(u)/sigma_eff by the exact integer division (per-cell reciprocal)
-#endif
-#ifndef BGS_RECIP_DIV
-#define BGS_RECIP_DIV 0   // face distances: division by the direction's stored reciprocals (div_recip)
-#endif
-#ifndef BGS_RECIP_DIV_DS
-#define BGS_RECIP_DIV_DS 1  // -log(u)/sigma_eff: division by the cell's stored reciprocal
-#endif
-#ifndef BGS_APPROX_FACES
-#define BGS_APPROX_FACES 1  // order the three face distances in single precision, divide once
-#endif
-#ifndef BGS_LANE_E0
-#define BGS_LANE_E0 0  // the birth weight E0 kept in registers (else read from the bank when needed)
-#endif
-#ifndef BGS_LANE_FACES
-// the face planes ahead kept in registers (else read from the mesh per
-// segment); the default of the kFaces template argument below, which a
-// kernel may set for itself
-#define BGS_LANE_FACES 0
-#endif
-#ifndef BGS_APPROX_CVT_HW
-#define BGS_APPROX_CVT_HW 0  // single-precision images by the conversion instruction (else by bits)
 #endif
 
 
@@ -65,44 +31,13 @@ __device__ __forceinline__ double div_recip(double a, double b, double y) {
   return __fma_rn(r, y, q0);
 }
 
-#if BGS_INT_DIV
-using DivRecip = unsigned long long;  // fix::divisor_recip of the direction cosine
-#else
-using DivRecip = double;              // RN(1/direction cosine) (recip_for_div)
-#endif
-
-__device__ __forceinline__ double seg_div(double a, double b, DivRecip rb) {
-#if BGS_INT_DIV
-  return fix::div_rn(a, b, rb);
-#elif BGS_RECIP_DIV
-  return div_recip(a, b, rb);
-#else
-  (void)rb;
-  return a / b;
-#endif
-}
-__device__ __forceinline__ double seg_sqrt(double x) {
-#if BGS_INT_SQRT
-  return fix::sqrt_rn(x);
-#else
-  return sqrt(x);
-#endif
-}
-__device__ __forceinline__ void seg_sincos(double phi, double *s, double *c) {
-#if BGS_INT_SINCOS
-  fix::sincos_phi(phi, s, c);
-#else
-  sincos(phi, s, c);
-#endif
-}
-
+// One history's state in registers.  The birth weight E0 is not kept: the
+// cutoff runs against RN(0.01 E0), and the rare exact test reads E0 from the
+// bank.  The face planes ahead are kept only by kernels that ask for them
+// (kFaces); the others read them from the mesh planes per segment.
 struct Lane {
   double px, py, pz, dx, dy, dz, E, life;
-#if BGS_LANE_E0
-  double E0;
-#endif
   double kill_thr;  // RN(0.01 * E0): the cutoff test runs against it in integer ulps
-  DivRecip rbx, rby, rbz;  // divisor reciprocals of the direction cosines
   double fx, fy, fz;  // the current cell's face planes ahead along x, y, z (kFaces)
   double thr_abs;   // absorbed energy of the current cell visit
   double thr_trk;   // the visit's track tally, set by a cutoff kill (visit_track)
@@ -114,7 +49,7 @@ struct Lane {
 // the node planes the photon moves toward along each axis: the upper one
 // for a positive direction cosine, else the lower one (the faces
 // get_distance_to_boundary measures to, cell.h:117-132)
-template <bool kFaces = BGS_LANE_FACES>
+template <bool kFaces = false>
 __device__ __forceinline__ void load_faces(const MeshDev &m, Lane &L) {
   if constexpr (kFaces) {
     L.fx = m.x[L.ci + ((__double_as_longlong(L.dx) > 0) ? 1u : 0u)];
@@ -123,13 +58,8 @@ __device__ __forceinline__ void load_faces(const MeshDev &m, Lane &L) {
   }
 }
 
-// a history's birth weight: E0 and the cutoff threshold RN(0.01 E0)
-__device__ __forceinline__ void set_birth(Lane &L, double E0) {
-#if BGS_LANE_E0
-  L.E0 = E0;
-#endif
-  L.kill_thr = kCutoff * E0;
-}
+// a history's birth weight: the cutoff threshold RN(0.01 E0)
+__device__ __forceinline__ void set_birth(Lane &L, double E0) { L.kill_thr = kCutoff * E0; }
 
 __device__ __forceinline__ void flush_tally(const CellsDev &c, const DeviceDiag *d, uint32_t cell,
                                             double a, double t, uint32_t &flags, int sa, int st) {
@@ -194,19 +124,6 @@ __device__ __forceinline__ void flush_tally_warp(TallyCell *tally, bool flush, K
   }
 }
 
-__device__ __forceinline__ void direction_recips(Lane &L) {
-#if BGS_INT_DIV
-  L.rbx = fix::divisor_recip(L.dx);
-  L.rby = fix::divisor_recip(L.dy);
-  L.rbz = fix::divisor_recip(L.dz);
-#elif BGS_RECIP_DIV
-  L.rbx = recip_for_div(L.dx);
-  L.rby = recip_for_div(L.dy);
-  L.rbz = recip_for_div(L.dz);
-#else
-  (void)L;
-#endif
-}
 
 __device__ __forceinline__ void store_end(const Bank &b, const Lane &L, uint8_t desc) {
   const unsigned long long i = L.idx;
@@ -262,11 +179,6 @@ __device__ __forceinline__ double visit_track(const CellXS &xs, const Lane &L, i
 __device__ __forceinline__ bool f32_image(double x, float &f) {
   const unsigned long long u = (unsigned long long)__double_as_longlong(x);
   const bool zero = (u << 1) == 0;
-#if BGS_APPROX_CVT_HW
-  f = __double2float_rz(x);
-  const float m = fabsf(f);
-  return zero || (m >= 1.17549435e-38f && m < 3.0e38f);
-#else
   const unsigned hi = (unsigned)(u >> 32), lo = (unsigned)u;
   const unsigned mag = hi & 0x7FFFFFFFu;
   // exponent field e in [897, 1150] is float's normal range: the float's
@@ -274,7 +186,6 @@ __device__ __forceinline__ bool f32_image(double x, float &f) {
   const unsigned bits = __funnelshift_l(lo, mag - (896u << 20), 3) | (hi & 0x80000000u);
   f = zero ? 0.0f : __uint_as_float(bits);
   return zero || (mag - (897u << 20)) < ((1151u - 897u) << 20);
-#endif
 }
 
 // The face that get_distance_to_boundary picks (cell.h:117-132), decided
@@ -333,24 +244,16 @@ struct SegInfo {
 // faces and to census, implicit-capture decay and track tally, the move, and
 // the cutoff test (history_based_transport.h:56-91).  On SEG_KILLED the
 // remaining energy has been added to the cell's absorbed energy, as upstream.
-template <bool kFaces = BGS_LANE_FACES>
+template <bool kFaces = false>
 __device__ __forceinline__ int segment_advance(const MeshDev &m, const double *E0s, const CellXS &xs, Lane &L,
                                                uint32_t &surface_cross, uint32_t &flags,
                                                SegInfo *info = nullptr) {
   ++L.segs;
   const bool scatters = f64_positive(xs.sig_eff);
-#if BGS_INT_DIV_DS
-  const double dist_to_scatter =
-      scatters ? fix::div_rn(fix::neg_log_u53(L.rng.next_m53()), xs.sig_eff, xs.rb_sig) : 1.0e100;
-#elif BGS_RECIP_DIV_DS
   // -log(u) / sigma_eff with the integer, correctly rounded -log
   // (bgs_fixmath.cuh) and the division by the cell's stored reciprocal
   const double dist_to_scatter =
       scatters ? div_recip(fix::neg_log_u53(L.rng.next_m53()), xs.sig_eff, xs.inv_se) : 1.0e100;
-#else
-  // -log(u) / sigma_eff with the integer, correctly rounded -log (bgs_fixmath.cuh)
-  const double dist_to_scatter = scatters ? fix::neg_log_u53(L.rng.next_m53()) / xs.sig_eff : 1.0e100;
-#endif
   // Cell::get_distance_to_boundary (cell.h:117-132): the first face with
   // the smallest (face - pos)/dir below 1e16, else 1e16 and face 0.  The
   // comparisons are the upstream ones, evaluated on the integer keys.
@@ -368,18 +271,14 @@ __device__ __forceinline__ int segment_advance(const MeshDev &m, const double *E
     ay = m.y[L.cj + (posy ? 1u : 0u)] - L.py;
     az = m.z[L.ck + (posz ? 1u : 0u)] - L.pz;
   }
-  bool decided = false;
-#if BGS_APPROX_FACES
-  decided = approx_faces(ax, ay, az, L, posx, posy, posz, dist_to_boundary, k_boundary, surface_cross);
-#endif
-  if (!decided) {
-    double dist = seg_div(ax, L.dx, L.rbx);
+  if (!approx_faces(ax, ay, az, L, posx, posy, posz, dist_to_boundary, k_boundary, surface_cross)) {
+    double dist = ax / L.dx;
     long long k = f64_key(dist);
     if (k < k_boundary) { dist_to_boundary = dist; k_boundary = k; surface_cross = posx ? 1u : 0u; }
-    dist = seg_div(ay, L.dy, L.rby);
+    dist = ay / L.dy;
     k = f64_key(dist);
     if (k < k_boundary) { dist_to_boundary = dist; k_boundary = k; surface_cross = posy ? 3u : 2u; }
-    dist = seg_div(az, L.dz, L.rbz);
+    dist = az / L.dz;
     k = f64_key(dist);
     if (k < k_boundary) { dist_to_boundary = dist; k_boundary = k; surface_cross = posz ? 5u : 4u; }
   }
@@ -411,12 +310,7 @@ __device__ __forceinline__ int segment_advance(const MeshDev &m, const double *E
   // closer than that the exact quotient settles it
   const long long k_e = f64_key(L.E), k_thr = f64_key(L.kill_thr);
   bool killed = k_e < k_thr;
-#if BGS_LANE_E0
-  (void)E0s;
-  if (k_e - k_thr <= 4 && k_thr - k_e <= 4) killed = L.E / L.E0 < kCutoff;
-#else
   if (k_e - k_thr <= 4 && k_thr - k_e <= 4) killed = L.E / E0s[L.idx] < kCutoff;
-#endif
   if (killed || L.segs >= kMaxSegmentsPerHistory) {
     if (!killed) flags |= FLAG_SEGMENT_LIMIT;
     L.thr_trk = L.thr_abs * xs.inv_saf;  // the visit's track tally, before the kill deposit
@@ -431,18 +325,17 @@ __device__ __forceinline__ int segment_advance(const MeshDev &m, const double *E
 // Effective scatter (history_based_transport.h:96-99): isotropic new
 // direction (get_uniform_angle, sampling_functions.h:57-70) and, unless
 // physical scattering wins, a resampled group.
-template <bool kFaces = BGS_LANE_FACES>
+template <bool kFaces = false>
 __device__ __forceinline__ void scatter_update(const MeshDev &m, const CellsDev &c, const CellXS &xs,
                                                Lane &L) {
   const double mu = mu_from_m53(L.rng.next_m53());
   const double phi = L.rng.next() * 2.0 * kPi;
-  const double sin_theta = seg_sqrt(1.0 - mu * mu);
+  const double sin_theta = fix::sqrt_rn(1.0 - mu * mu);
   double sp, cp;
-  seg_sincos(phi, &sp, &cp);
+  fix::sincos_phi(phi, &sp, &cp);
   L.dx = sin_theta * cp;
   L.dy = sin_theta * sp;
   L.dz = mu;
-  direction_recips(L);
   load_faces<kFaces>(m, L);
   // effective-scatter test and group resample (history_based_transport.h:97-98):
   // with sigma_s = 0 the test u > 0 always passes, and with one group the
@@ -473,7 +366,7 @@ __device__ __forceinline__ int face_bc(const MeshDev &m, const Lane &L, uint32_t
 
 // ELEMENT crossing: the photon enters the neighbour (cell.h:110-112); only
 // the crossed axis gets a new face ahead
-template <bool kFaces = BGS_LANE_FACES>
+template <bool kFaces = false>
 __device__ __forceinline__ void enter_neighbour(const MeshDev &m, Lane &L, uint32_t surface_cross) {
   switch (surface_cross) {
     case 0: --L.ci; L.cell -= 1; if constexpr (kFaces) L.fx = m.x[L.ci]; break;
@@ -487,33 +380,22 @@ __device__ __forceinline__ void enter_neighbour(const MeshDev &m, Lane &L, uint3
 
 // REFLECT: Photon::reflect (photon.h:151-155): the direction cosine flips
 // and the face ahead on that axis becomes the opposite plane of the cell.
-// An integer divisor reciprocal depends only on the magnitude; RN(1/-b) =
-// -RN(1/b) exactly.
-template <bool kFaces = BGS_LANE_FACES>
+template <bool kFaces = false>
 __device__ __forceinline__ void reflect(const MeshDev &m, Lane &L, uint32_t surface_cross) {
   if (surface_cross < 2) {
     L.dx = -L.dx;
-#if !BGS_INT_DIV
-    L.rbx = -L.rbx;
-#endif
     if constexpr (kFaces) L.fx = m.x[L.ci + ((__double_as_longlong(L.dx) > 0) ? 1u : 0u)];
   } else if (surface_cross < 4) {
     L.dy = -L.dy;
-#if !BGS_INT_DIV
-    L.rby = -L.rby;
-#endif
     if constexpr (kFaces) L.fy = m.y[L.cj + ((__double_as_longlong(L.dy) > 0) ? 1u : 0u)];
   } else {
     L.dz = -L.dz;
-#if !BGS_INT_DIV
-    L.rbz = -L.rbz;
-#endif
     if constexpr (kFaces) L.fz = m.z[L.ck + ((__double_as_longlong(L.dz) > 0) ? 1u : 0u)];
   }
 }
 
 // cell coordinates and the faces ahead from the global cell index
-template <bool kFaces = BGS_LANE_FACES>
+template <bool kFaces = false>
 __device__ __forceinline__ void locate(const MeshDev &m, Lane &L) {
   L.ci = L.cell % m.ngx;
   L.cj = (L.cell / m.ngx) % m.ngy;

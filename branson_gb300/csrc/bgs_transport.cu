@@ -67,7 +67,6 @@ __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
             L.thr_abs = 0.0;
           }
           set_birth(L, b.E0[i]);
-          direction_recips(L);
           if (L.cell < m.n_cells) {
             locate(m, L);
             active = true;

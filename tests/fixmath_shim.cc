@@ -29,7 +29,5 @@ void libm_sincos(double phi, double *s, double *c) {
 }
 }
 extern "C" {
-uint64_t fix_recip116(uint64_t m) { return bgs::fix::recip116(m); }
-double fix_div(double a, double b) { return bgs::fix::div_rn(a, b, bgs::fix::divisor_recip(b)); }
 double fix_sqrt(double x) { return bgs::fix::sqrt_rn(x); }
 }

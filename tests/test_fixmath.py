@@ -4,7 +4,6 @@ rounding) and the host libm (what the upstream CPU code calls)."""
 import ctypes as C
 import os
 import subprocess
-import tempfile
 
 import numpy as np
 import pytest
@@ -16,7 +15,9 @@ _lib = None
 def shim():
     global _lib
     if _lib is None:
-        out = os.path.join(tempfile.mkdtemp(), "fixshim.so")
+        out_dir = os.path.join(ROOT, "branson_gb300", "_build")  # git-ignored build folder
+        os.makedirs(out_dir, exist_ok=True)
+        out = os.path.join(out_dir, "fixshim.so")
         cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
                "-I", os.path.join(ROOT, "branson_gb300", "csrc"),
                os.path.join(ROOT, "tests", "fixmath_shim.cc"), "-o", out, "-lquadmath"]
@@ -120,38 +121,8 @@ def test_sincos_correctly_rounded():
 
 
 def _bind_exact(L):
-    L.fix_div.restype = C.c_double
-    L.fix_div.argtypes = [C.c_double, C.c_double]
     L.fix_sqrt.restype = C.c_double
     L.fix_sqrt.argtypes = [C.c_double]
-    L.fix_recip116.restype = C.c_uint64
-    L.fix_recip116.argtypes = [C.c_uint64]
-
-
-def test_recip116_is_exact_floor():
-    L = shim()
-    _bind_exact(L)
-    rng = np.random.default_rng(4)
-    Ms = list(range(2 ** 52 + 1, 2 ** 52 + 3000)) + list(range(2 ** 53 - 3000, 2 ** 53)) + \
-        [int(v) for v in rng.integers(2 ** 52 + 1, 2 ** 53, 20000, dtype=np.uint64)]
-    bad = [M for M in Ms if L.fix_recip116(M) != (1 << 116) // M]
-    assert not bad, bad[:5]
-
-
-def test_division_matches_ieee_bitwise():
-    """Signs, powers of two and mantissas next to them, tiny/large ratios."""
-    L = shim()
-    _bind_exact(L)
-    rng = np.random.default_rng(5)
-    a = 10.0 ** rng.uniform(-12, 6, 100000) * rng.choice([-1.0, 1.0], 100000)
-    b = 10.0 ** rng.uniform(-6, 6, 100000) * rng.choice([-1.0, 1.0], 100000)
-    edge = np.array([np.nextafter(2.0 ** k, s) for k in range(-30, 30) for s in (0.0, 1e300)] +
-                    [2.0 ** k for k in range(-30, 30)])
-    a = np.concatenate([a, rng.uniform(0.1, 10, edge.size * 20), [0.0, -0.0, 1.0]])
-    b = np.concatenate([b, np.repeat(edge, 20), [3.0, 3.0, 3.0]])
-    got = np.array([L.fix_div(x, y) for x, y in zip(a, b)])
-    ref = a / b
-    assert np.array_equal(got.view(np.int64), ref.view(np.int64))
 
 
 def test_sqrt_matches_ieee_bitwise():
