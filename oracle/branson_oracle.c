@@ -787,10 +787,10 @@ static double adjoint_replay_photon(const bo_mesh *m, const bo_cells *c, const b
       const double gs = a.g2 * s;
       const double pa = a.f2 * d;
       const double prev = prefix;
-      prefix = prefix + wj * absorbed_E;
-      const double tail = prefix + wj * p->E;
+      prefix = fma(wj, absorbed_E, prefix);
+      const double tail = fma(wj, p->E, prefix);
       vis_a = vis_a + (gs - pa);
-      vis_b = vis_b + (gs * prev - pa * tail);
+      vis_b = fma(gs, prev, fma(-pa, tail, vis_b));
       if (killed) prefix = tail;
       if (op_a_p) {
         const double sp = op_a_p[cell], fp = f_p[cell];
