@@ -549,8 +549,9 @@ int bgs_set_photons(bgs_context *ctx, uint64_t count, const bgs_photons_host *in
   if (count > ctx->capacity)
     return fail(ctx, BGS_ERR_CAPACITY, "%llu photons exceed the bank capacity %llu",
                 (unsigned long long)count, ctx->capacity);
-  if (!in->pos_x || !in->pos_y || !in->pos_z || !in->dir_x || !in->dir_y || !in->dir_z || !in->E ||
-      !in->E0 || !in->life_dx || !in->cell || !in->group || !in->rng_stream || !in->rng_counter)
+  if (count > 0 && (!in->pos_x || !in->pos_y || !in->pos_z || !in->dir_x || !in->dir_y || !in->dir_z ||
+                    !in->E || !in->E0 || !in->life_dx || !in->cell || !in->group || !in->rng_stream ||
+                    !in->rng_counter))
     return fail(ctx, BGS_ERR_INVALID, "input photons need every state array");
   int rc = set_device(ctx);
   if (rc) return rc;
