@@ -103,6 +103,16 @@ __device__ __forceinline__ void source_angle(Rng &r, int face, double d[3]) {
   }
 }
 
+// the photon's group, floor(u * n_groups) (source.h:94, :111, :128); with one
+// group it is 0 whatever u is, so that draw only advances the counter
+__device__ __forceinline__ uint32_t sample_uniform_group(Rng &r, uint32_t n_groups) {
+  if (n_groups == 1) {
+    r.skip();
+    return 0u;
+  }
+  return (uint32_t)floor(r.next() * (double)n_groups);
+}
+
 // index of the cell whose [off[c], off[c+1]) range holds p
 __device__ __forceinline__ uint32_t find_cell(const unsigned long long *off, uint32_t n_cells,
                                               unsigned long long p) {
@@ -141,7 +151,7 @@ __device__ __forceinline__ void source_census_body(const MeshDev &m, const Cells
     position_in_cell(nodes, r, pos);
     uniform_angle(r, dir);
     const double E = c.ce_E[g] / (double)c.n_ce[g];
-    const uint32_t group = (uint32_t)floor(r.next() * (double)m.n_groups);
+    const uint32_t group = sample_uniform_group(r, m.n_groups);
     store_photon(b, p, pos, dir, E, kC * dt, g, group, 0, p, r.ctr);
   }
 }
@@ -182,7 +192,7 @@ __device__ __forceinline__ void source_new_body(const MeshDev &m, const CellsDev
       stype = 1;
     }
     const double life = r.next() * kC * dt;
-    const uint32_t group = (uint32_t)floor(r.next() * (double)m.n_groups);
+    const uint32_t group = sample_uniform_group(r, m.n_groups);
     store_photon(b, base + p, pos, dir, E, life, g, group, stype, stream, r.ctr);
   }
 }
