@@ -31,14 +31,11 @@
 #include "bgs_fixmath_tables.h"
 
 #if defined(__CUDACC__)
+// every routine inlined into its caller: calls (argument moves, saved
+// registers, the return) measured slower than the larger loop body
 #define BGS_HD __host__ __device__ __forceinline__
-// one shared copy in device code: routines called from several places of
-// the transport loop are kept out of line so the loop fits the instruction
-// cache
-#define BGS_HD_SHARED static __host__ __device__ __noinline__
 #else
 #define BGS_HD inline
-#define BGS_HD_SHARED inline
 #endif
 
 namespace bgs {
@@ -117,7 +114,7 @@ BGS_HD uint64_t double_to_bits(double d) {
 // Round the positive value W * 2^-scale (W != 0) to the nearest double.
 // Values below the normal range flush to zero (callers never produce them
 // on the paths that use this).
-BGS_HD_SHARED double round_u128(u128 W, int scale) {
+BGS_HD double round_u128(u128 W, int scale) {
   const uint64_t hi = (uint64_t)(W >> 64), lo = (uint64_t)W;
   const int p = hi ? 127 - clz64(hi) : 63 - clz64(lo);  // top set bit
   uint64_t mant;
