@@ -382,7 +382,8 @@ BGS_HD double sqrt_rn(double x) {
   const float rsf = 1.0f / std::sqrt(wf);
 #endif
   uint64_t R = float_to_fixed(rsf, 62);  // r = 1/sqrt(w) in (1, 2], Q62
-#pragma unroll 1
+  // two Newton steps r <- r (3 - w r^2)/2: 23 -> ~46 -> ~62 bits
+#pragma unroll
   for (int it = 0; it < 2; ++it) {
     const uint64_t R2 = (uint64_t)(((u128)R * R) >> 64);   // r^2, Q60
     const uint64_t wr2 = mulhi(W, R2);                       // w r^2, Q60 (~2^60)
@@ -390,12 +391,20 @@ BGS_HD double sqrt_rn(double x) {
     R = (uint64_t)(((u128)R * t) >> 61);                     // r (3 - w r^2)/2, Q62
   }
   uint64_t y = mulhi(W, R) >> 9;  // sqrt(w) * 2^53 ~ floor(sqrt(N))
+  // exact floor(sqrt(N)) from one square: (y -+ 1)^2 = y^2 -+ (2y -+ 1)
+  u128 sq = (u128)y * y;
 #pragma unroll 1
-  for (int it = 0; it < 8 && (u128)y * y > N; ++it) --y;
+  for (int it = 0; it < 8 && sq > N; ++it) {
+    sq -= (u128)(2 * y - 1);
+    --y;
+  }
 #pragma unroll 1
-  for (int it = 0; it < 8 && (u128)(y + 1) * (y + 1) <= N; ++it) ++y;
+  for (int it = 0; it < 8 && sq + (u128)(2 * y + 1) <= N; ++it) {
+    sq += (u128)(2 * y + 1);
+    ++y;
+  }
   // nearest: N - y^2 > y  <=>  sqrt(N) > y + 1/2 (no exact ties)
-  if (N - (u128)y * y > (u128)y) ++y;
+  if (N - sq > (u128)y) ++y;
   int eo = (e - 52) / 2 + 52;  // value = y * 2^(eo - 52)
   if (y >> 53) { y >>= 1; ++eo; }
   return bits_to_double(((uint64_t)(eo + 1023) << 52) | (y & 0x000FFFFFFFFFFFFFULL));
