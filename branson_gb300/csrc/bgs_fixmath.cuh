@@ -139,6 +139,36 @@ BGS_HD double round_u128(u128 W, int scale) {
   return bits_to_double(((uint64_t)be << 52) | (mant & 0x000FFFFFFFFFFFFFULL));
 }
 
+// round_u128 for a W whose top set bit is at 117 or above, so the mantissa
+// and the rounding position both lie in the high word (the sine and exp
+// results): one 64-bit shift and compare instead of 128-bit ones.
+BGS_HD double round_u128_high(u128 W, int scale) {
+  const uint64_t hi = (uint64_t)(W >> 64), lo = (uint64_t)W;
+  const int ph = 63 - clz64(hi);  // top set bit of W is ph + 64
+  const int sh = ph - 52;         // bits of hi below the mantissa, >= 1
+  uint64_t mant = hi >> sh;
+  const uint64_t rem = hi & ((1ULL << sh) - 1), half = 1ULL << (sh - 1);
+  const bool up = rem > half || (rem == half && (lo != 0 || (mant & 1)));
+  int e2 = ph + 64 - scale;  // value = mant * 2^(e2 - 52)
+  if (up) {
+    ++mant;
+    if (mant >> 53) { mant >>= 1; ++e2; }
+  }
+  const int be = e2 + 1023;
+  if (be <= 0) return 0.0;
+  return bits_to_double(((uint64_t)be << 52) | (mant & 0x000FFFFFFFFFFFFFULL));
+}
+
+// v * 2^-64 for v in [2^63, 2^64) rounded to the nearest double (the cosine
+// on [0, pi/4], as 1 - cb)
+BGS_HD double round_unit_q64(uint64_t v) {
+  uint64_t mant = v >> 11;
+  const uint64_t rem = v & 0x7FFULL;
+  mant += (rem > 0x400ULL || (rem == 0x400ULL && (mant & 1))) ? 1ULL : 0ULL;
+  if (mant >> 53) return 1.0;  // rounded up to the value 1
+  return bits_to_double((1022ULL << 52) | (mant & 0x000FFFFFFFFFFFFFULL));
+}
+
 // -ln(u) for the RNG draw u = m * 2^-53 (u01fixedpt: m odd, 1 <= m < 2^53).
 // The result is the value -log(u) rounds to (the upstream distance to
 // collision numerator, history_based_transport.h:62-63).
@@ -224,7 +254,7 @@ BGS_HD double exp_neg(double tau) {
     const uint64_t P = (uint64_t)0 - sb;  // (1 - s b) * 2^64
     W = (u128)E * P;
   }
-  return round_u128(W, 127 + (int)q);
+  return round_u128_high(W, 127 + (int)q);  // W in (2^125, 2^127]
 }
 
 
@@ -303,12 +333,12 @@ BGS_HD SinCos sincos_phi_v(double phi) {
     for (int k = 8; k >= 0; --k) b = kS[k] - mulhi(y, b);   // 1/3! - y(1/5! - ...)
     const uint64_t sb = mulhi(y, b);                          // y * b
     const u128 Ws = sb ? (u128)Tm * ((uint64_t)0 - sb) : ((u128)Tm << 64);
-    sv = round_u128(Ws, 122 + lz);
+    sv = round_u128_high(Ws, 122 + lz);  // Ws in [2^124, 2^127)
     uint64_t c = kCo[9];
 #pragma unroll
     for (int k = 8; k >= 0; --k) c = kCo[k] - mulhi(y, c);  // 1/2! - y(1/4! - ...)
     const uint64_t cb = mulhi(y, c);
-    cv = cb ? round_u128((u128)((uint64_t)0 - cb), 64) : 1.0;
+    cv = cb ? round_unit_q64((uint64_t)0 - cb) : 1.0;  // cos >= cos(pi/4): 2^64 - cb >= 2^63
   }
   const double so = swap ? cv : sv;  // sin, cos of (t*pi/2)
   const double co = swap ? sv : cv;
