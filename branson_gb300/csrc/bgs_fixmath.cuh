@@ -265,10 +265,6 @@ BGS_HD double exp_neg(double tau) {
 // Taylor polynomials in fixed point; the small one of the pair is always a
 // sine computed relative to its argument, so tiny results keep full
 // precision.  Results are rounded to nearest.
-BGS_HD double round_u64_scaled(uint64_t mant_hi, uint64_t mant_lo, int scale) {
-  return round_u128(((u128)mant_hi << 64) | mant_lo, scale);
-}
-
 struct SinCos {
   double s, c;
 };
