@@ -208,10 +208,6 @@ struct Rng {
   }
   // advance past a draw whose value cannot change the result
   __device__ __forceinline__ void skip() { ++ctr; }
-  // raw output word of the draw k positions ahead (counter not advanced)
-  __device__ __forceinline__ unsigned long long peek(unsigned k) const {
-    return threefry2x64_20_w0(ctr + k, hi, stream);
-  }
   // the integer m of the next draw u = m * 2^-53 (u01fixedpt, RNG.h:202-238)
   __device__ __forceinline__ unsigned long long next_m53() {
     const unsigned long long w = threefry2x64_20_w0(ctr, hi, stream);

@@ -1,6 +1,7 @@
 // Per-segment physics of transport_photon (history_based_transport.h:55-139),
-// shared by the history kernel (bgs_transport.cu) and the event-mode stage
-// kernels (bgs_event.cu) so both run the identical arithmetic.
+// shared by the history kernel (bgs_transport.cu), the batched kernel
+// (bgs_batch.cu), the event-mode stage kernels (bgs_event.cu) and the adjoint
+// replay (bgs_adjoint.cu), so all of them run the identical arithmetic.
 #pragma once
 
 #include "bgs_fixmath.cuh"
@@ -60,21 +61,6 @@ __device__ __forceinline__ void load_faces(const MeshDev &m, Lane &L) {
 
 // a history's birth weight: the cutoff threshold RN(0.01 E0)
 __device__ __forceinline__ void set_birth(Lane &L, double E0) { L.kill_thr = kCutoff * E0; }
-
-__device__ __forceinline__ void flush_tally(const CellsDev &c, const DeviceDiag *d, uint32_t cell,
-                                            double a, double t, uint32_t &flags, int sa, int st) {
-  unsigned long long lo, hi;
-  TallyCell *tc = &c.tally[cell];
-  // nonzero tests on the bit patterns (either sign of zero is zero)
-  if ((__double_as_longlong(a) << 1) != 0) {
-    if (to_fixed128(a, sa, lo, hi)) atomic_add128(&tc->abs_lo, &tc->abs_hi, lo, hi);
-    else flags |= (a == a) ? FLAG_TALLY_RANGE : FLAG_NAN;
-  }
-  if ((__double_as_longlong(t) << 1) != 0) {
-    if (to_fixed128(t, st, lo, hi)) atomic_add128(&tc->trk_lo, &tc->trk_hi, lo, hi);
-    else flags |= (t == t) ? FLAG_TALLY_RANGE : FLAG_NAN;
-  }
-}
 
 // Warp-aggregated tally flush: every lane of the warp calls it (flush false
 // for lanes with nothing to add); lanes flushing into the same cell
