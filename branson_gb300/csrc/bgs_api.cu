@@ -59,34 +59,55 @@ int alloc_bank(bgs_context *ctx, Bank &b, unsigned long long cap) {
 }
 
 // copy count photons between a bank (at offset) and host SoA arrays
+// photon fields of a host/device copy
+enum : unsigned {
+  F_POS = 1u, F_DIR = 2u, F_E = 4u, F_E0 = 8u, F_LIFE = 16u, F_CELL = 32u, F_GROUP = 64u, F_DESC = 128u,
+  F_STYPE = 256u, F_STREAM = 512u, F_CTR = 1024u, F_ALL = 2047u
+};
+
+// photons [offset, offset + n) of the bank and of the host arrays (the same
+// index in both), the fields in `fields` whose host pointer is set, on s
 int copy_photons(bgs_context *ctx, const Bank &b, unsigned long long offset, unsigned long long n,
-                 const bgs_photons_host *h, bool to_host) {
+                 const bgs_photons_host *h, bool to_host, cudaStream_t s, unsigned fields) {
   if (n == 0) return BGS_OK;
   const cudaMemcpyKind kind = to_host ? cudaMemcpyDeviceToHost : cudaMemcpyHostToDevice;
-#define BGS_CP(dev, host, T)                                                                    \
-  if (h->host) {                                                                                \
-    if (to_host)                                                                                \
-      BGS_CUDA(ctx, cudaMemcpyAsync(h->host, b.dev + offset, n * sizeof(T), kind, ctx->stream)); \
-    else                                                                                        \
-      BGS_CUDA(ctx, cudaMemcpyAsync(b.dev + offset, h->host, n * sizeof(T), kind, ctx->stream)); \
+#define BGS_CP(dev, host, T, F)                                                                           \
+  if (h->host && (fields & (F))) {                                                                        \
+    if (to_host)                                                                                          \
+      BGS_CUDA(ctx, cudaMemcpyAsync(h->host + offset, b.dev + offset, n * sizeof(T), kind, s));           \
+    else                                                                                                  \
+      BGS_CUDA(ctx, cudaMemcpyAsync(b.dev + offset, h->host + offset, n * sizeof(T), kind, s));           \
   }
-  BGS_CP(px, pos_x, double)
-  BGS_CP(py, pos_y, double)
-  BGS_CP(pz, pos_z, double)
-  BGS_CP(dx, dir_x, double)
-  BGS_CP(dy, dir_y, double)
-  BGS_CP(dz, dir_z, double)
-  BGS_CP(E, E, double)
-  BGS_CP(E0, E0, double)
-  BGS_CP(life, life_dx, double)
-  BGS_CP(cell, cell, uint32_t)
-  BGS_CP(group, group, uint32_t)
-  BGS_CP(desc, descriptor, uint8_t)
-  BGS_CP(stype, source_type, uint8_t)
-  BGS_CP(stream, rng_stream, uint64_t)
-  BGS_CP(ctr, rng_counter, uint64_t)
+  BGS_CP(px, pos_x, double, F_POS)
+  BGS_CP(py, pos_y, double, F_POS)
+  BGS_CP(pz, pos_z, double, F_POS)
+  BGS_CP(dx, dir_x, double, F_DIR)
+  BGS_CP(dy, dir_y, double, F_DIR)
+  BGS_CP(dz, dir_z, double, F_DIR)
+  BGS_CP(E, E, double, F_E)
+  BGS_CP(E0, E0, double, F_E0)
+  BGS_CP(life, life_dx, double, F_LIFE)
+  BGS_CP(cell, cell, uint32_t, F_CELL)
+  BGS_CP(group, group, uint32_t, F_GROUP)
+  BGS_CP(desc, descriptor, uint8_t, F_DESC)
+  BGS_CP(stype, source_type, uint8_t, F_STYPE)
+  BGS_CP(stream, rng_stream, uint64_t, F_STREAM)
+  BGS_CP(ctr, rng_counter, uint64_t, F_CTR)
 #undef BGS_CP
   return BGS_OK;
+}
+
+// the whole photon state on the context's stream: host arrays [0, n) at bank [offset, offset + n)
+int copy_photons(bgs_context *ctx, const Bank &b, unsigned long long offset, unsigned long long n,
+                 const bgs_photons_host *h, bool to_host) {
+  if (offset == 0) return copy_photons(ctx, b, 0, n, h, to_host, ctx->stream, F_ALL);
+  Bank shifted = b;  // host index 0 is bank index offset
+  shifted.px += offset; shifted.py += offset; shifted.pz += offset;
+  shifted.dx += offset; shifted.dy += offset; shifted.dz += offset;
+  shifted.E += offset; shifted.E0 += offset; shifted.life += offset;
+  shifted.cell += offset; shifted.group += offset; shifted.desc += offset; shifted.stype += offset;
+  shifted.stream += offset; shifted.ctr += offset;
+  return copy_photons(ctx, shifted, 0, n, h, to_host, ctx->stream, F_ALL);
 }
 
 __global__ void k_set_bank_size(DeviceDiag *d, unsigned long long n) {
@@ -105,6 +126,96 @@ __global__ void k_reset_queue(DeviceDiag *d) {
 // the history tail after event rounds restarts the work queue only; the
 // segments the event stages counted stay in the step's total
 __global__ void k_reset_work(DeviceDiag *d) { d->work_counter = 0; }
+
+}  // namespace
+
+namespace {
+
+// Drop-in transport of a large host bank as a pipeline: the weights and
+// flights go first (the fixed-point scales need the whole bank's maxima),
+// the rest of the state follows in chunks on a copy stream, and each chunk
+// is transported as soon as it is on the device, alternating two compute
+// streams so one chunk's tail overlaps the next chunk; each chunk's end
+// states (all but life_dx, which the census pass resets) go back while the
+// later chunks run.  Results are those of one launch over the whole bank:
+// every photon owns its RNG stream and the tallies are exact fixed-point
+// sums.
+int pipe_setup(bgs_context *ctx) {
+  if (ctx->copy_stream) return BGS_OK;
+  BGS_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+  BGS_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking));
+  for (cudaEvent_t *e : {&ctx->pipe_start, &ctx->pipe_prep, &ctx->pipe_aux, &ctx->pipe_back})
+    BGS_CUDA(ctx, cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  for (int k = 0; k < bgs_context::kPipeChunks; ++k) {
+    BGS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->pipe_in[k], cudaEventDisableTiming));
+    BGS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->pipe_done[k], cudaEventDisableTiming));
+  }
+  return dev_alloc(ctx, ctx->pipe_allocs, &ctx->pipe_queue, (size_t)bgs_context::kPipeChunks);
+}
+
+int transport_pipelined(bgs_context *ctx, uint64_t n, const bgs_photons_host *in, double next_dt) {
+  int rc;
+  if ((rc = pipe_setup(ctx))) return rc;
+  Bank &b = ctx->bank[ctx->cur];
+  cudaStream_t s = ctx->stream, cs = ctx->copy_stream, as = ctx->aux_stream;
+  constexpr int K = bgs_context::kPipeChunks;
+  const uint64_t chunk = (n + K - 1) / K;
+  const uint64_t before = ctx->launches;
+  // nothing may touch the bank before the context's earlier work is done
+  BGS_CUDA(ctx, cudaEventRecord(ctx->pipe_start, s));
+  BGS_CUDA(ctx, cudaStreamWaitEvent(cs, ctx->pipe_start, 0));
+  BGS_CUDA(ctx, cudaStreamWaitEvent(as, ctx->pipe_start, 0));
+  // weights and flights, then the scales from their maxima
+  if ((rc = copy_photons(ctx, b, 0, n, in, false, s, F_E | F_LIFE))) return rc;
+  if (!in->descriptor) BGS_CUDA(ctx, cudaMemsetAsync(b.desc, PASS, n, s));
+  if (!in->source_type) BGS_CUDA(ctx, cudaMemsetAsync(b.stype, 0, n, s));
+  k_set_bank_size<<<1, 1, 0, s>>>(ctx->d_diag, n);
+  BGS_LAUNCHED(ctx, 1);
+  if ((rc = prepare_transport(ctx, b))) return rc;
+  BGS_CUDA(ctx, cudaMemsetAsync(ctx->pipe_queue, 0, K * sizeof(unsigned long long), s));
+  BGS_CUDA(ctx, cudaEventRecord(ctx->pipe_prep, s));
+  // the rest of the state, chunk by chunk
+  const unsigned rest = F_ALL & ~(F_E | F_LIFE);
+  for (int k = 0; k < K; ++k) {
+    const uint64_t first = k * chunk, cnt = first < n ? (n - first < chunk ? n - first : chunk) : 0;
+    if ((rc = copy_photons(ctx, b, first, cnt, in, false, cs, rest))) return rc;
+    BGS_CUDA(ctx, cudaEventRecord(ctx->pipe_in[k], cs));
+  }
+  // each chunk's transport once its state has arrived
+  BGS_CUDA(ctx, cudaStreamWaitEvent(as, ctx->pipe_prep, 0));
+  BGS_CUDA(ctx, cudaEventRecord(ctx->ev0, s));
+  for (int k = 0; k < K; ++k) {
+    const uint64_t first = k * chunk, cnt = first < n ? (n - first < chunk ? n - first : chunk) : 0;
+    cudaStream_t st = (k & 1) ? as : s;
+    BGS_CUDA(ctx, cudaStreamWaitEvent(st, ctx->pipe_in[k], 0));
+    if (cnt) {
+      launch_transport_history_range(ctx->mesh, ctx->cells, b, ctx->d_diag, ctx->seed, first, cnt,
+                                     ctx->pipe_queue + k, ctx->tshape, st);
+      BGS_LAUNCHED(ctx, 1);
+    }
+    BGS_CUDA(ctx, cudaEventRecord(ctx->pipe_done[k], st));
+  }
+  BGS_CUDA(ctx, cudaEventRecord(ctx->pipe_aux, as));
+  BGS_CUDA(ctx, cudaStreamWaitEvent(s, ctx->pipe_aux, 0));
+  BGS_CUDA(ctx, cudaEventRecord(ctx->ev1, s));
+  // end states back as chunks finish (life_dx after the census pass)
+  bgs_photons_host back = *in;
+  back.E0 = nullptr;  // unchanged by transport
+  back.rng_stream = nullptr;
+  back.source_type = nullptr;
+  for (int k = 0; k < K; ++k) {
+    const uint64_t first = k * chunk, cnt = first < n ? (n - first < chunk ? n - first : chunk) : 0;
+    BGS_CUDA(ctx, cudaStreamWaitEvent(cs, ctx->pipe_done[k], 0));
+    if ((rc = copy_photons(ctx, b, first, cnt, &back, true, cs, F_ALL & ~F_LIFE))) return rc;
+  }
+  BGS_CUDA(ctx, cudaEventRecord(ctx->pipe_back, cs));
+  if ((rc = finish_transport(ctx, next_dt))) return rc;
+  if ((rc = copy_photons(ctx, b, 0, n, &back, true, s, F_LIFE))) return rc;
+  BGS_CUDA(ctx, cudaStreamWaitEvent(s, ctx->pipe_back, 0));
+  ctx->bank_is_census = true;
+  ctx->last_launches = (uint32_t)(ctx->launches - before);
+  return BGS_OK;
+}
 
 }  // namespace
 
@@ -183,6 +294,15 @@ int bgs_destroy(bgs_context *ctx) {
   free_list(ctx->event_allocs);
   free_list(ctx->adj_allocs);
   free_list(ctx->comb_allocs);
+  free_list(ctx->pipe_allocs);
+  for (cudaEvent_t e : {ctx->pipe_start, ctx->pipe_prep, ctx->pipe_aux, ctx->pipe_back})
+    if (e) cudaEventDestroy(e);
+  for (int k = 0; k < bgs_context::kPipeChunks; ++k) {
+    if (ctx->pipe_in[k]) cudaEventDestroy(ctx->pipe_in[k]);
+    if (ctx->pipe_done[k]) cudaEventDestroy(ctx->pipe_done[k]);
+  }
+  if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+  if (ctx->aux_stream) cudaStreamDestroy(ctx->aux_stream);
   if (ctx->h_counter) cudaFreeHost(ctx->h_counter);
   if (ctx->d_diag) cudaFree(ctx->d_diag);
   if (ctx->h_diag) cudaFreeHost(ctx->h_diag);
@@ -574,15 +694,27 @@ int bgs_replicated_transport(bgs_context *ctx, uint64_t n, const bgs_photons_hos
   if (!ctx || !photons) return BGS_ERR_INVALID;
   if (!ctx->has_mesh) return fail(ctx, BGS_ERR_STATE, "no mesh");
   int rc;
-  if ((rc = bgs_set_photons(ctx, n, photons))) return rc;
-  if ((rc = transport_impl(ctx, next_dt, algorithm))) return rc;
-  // end states come back from the bank that was transported
-  const Bank &done = ctx->bank[1 - ctx->cur];
-  bgs_photons_host back = *photons;
-  back.E0 = nullptr;           // unchanged by transport
-  back.rng_stream = nullptr;
-  back.source_type = nullptr;
-  if ((rc = copy_photons(ctx, done, 0, n, &back, true))) return rc;
+  if (algorithm == BGS_HISTORY && ctx->pipe_min_photons > 0 && n >= ctx->pipe_min_photons && n > 0) {
+    if (n > ctx->capacity)
+      return fail(ctx, BGS_ERR_CAPACITY, "%llu photons exceed the bank capacity %llu", (unsigned long long)n,
+                  ctx->capacity);
+    if (!photons->pos_x || !photons->pos_y || !photons->pos_z || !photons->dir_x || !photons->dir_y ||
+        !photons->dir_z || !photons->E || !photons->E0 || !photons->life_dx || !photons->cell ||
+        !photons->group || !photons->rng_stream || !photons->rng_counter)
+      return fail(ctx, BGS_ERR_INVALID, "input photons need every state array");
+    if ((rc = set_device(ctx))) return rc;
+    if ((rc = transport_pipelined(ctx, n, photons, next_dt))) return rc;
+  } else {
+    if ((rc = bgs_set_photons(ctx, n, photons))) return rc;
+    if ((rc = transport_impl(ctx, next_dt, algorithm))) return rc;
+    // end states come back from the bank that was transported
+    const Bank &done = ctx->bank[1 - ctx->cur];
+    bgs_photons_host back = *photons;
+    back.E0 = nullptr;           // unchanged by transport
+    back.rng_stream = nullptr;
+    back.source_type = nullptr;
+    if ((rc = copy_photons(ctx, done, 0, n, &back, true))) return rc;
+  }
   if (rank_abs_E)
     BGS_CUDA(ctx, cudaMemcpyAsync(rank_abs_E, ctx->d_abs, ctx->mesh.n_cells * sizeof(double),
                                   cudaMemcpyDeviceToHost, ctx->stream));
@@ -625,6 +757,10 @@ int bgs_set_option(bgs_context *ctx, int option, double value) {
       ctx->transport_blocks = (int)value;
       ctx->tshape = transport_launch_shape(ctx->n_sm, ctx->tshape.threads);
       if (value > 0) ctx->tshape.blocks = (int)value;
+      return BGS_OK;
+    case BGS_OPT_PIPELINE_MIN_PHOTONS:
+      if (!(value >= 0 && value <= 1e15)) break;
+      ctx->pipe_min_photons = (unsigned long long)value;
       return BGS_OK;
     case BGS_OPT_TRANSPORT_THREADS:
       if (value != 64 && value != 128 && value != 256) break;

@@ -64,6 +64,16 @@ struct bgs_context {
   std::vector<unsigned long long> h_adj_item_off;
   unsigned long long mesh_generation = 0;  // bumped by every bgs_set_mesh
 
+  // pipelined drop-in transport (created on first use): a copy stream, a
+  // second compute stream, per-chunk events and work counters
+  static constexpr int kPipeChunks = 8;
+  unsigned long long pipe_min_photons = 1ULL << 20;  // 0: never pipelined
+  cudaStream_t copy_stream = nullptr, aux_stream = nullptr;
+  cudaEvent_t pipe_start = nullptr, pipe_prep = nullptr, pipe_aux = nullptr, pipe_back = nullptr;
+  cudaEvent_t pipe_in[kPipeChunks] = {}, pipe_done[kPipeChunks] = {};
+  unsigned long long *pipe_queue = nullptr;
+  std::vector<void *> pipe_allocs;
+
   // census comb (allocated on first use): radix-sort buffers, cell ranges
   std::vector<void *> comb_allocs;
   uint32_t *comb_keys = nullptr, *comb_pos = nullptr;  // 2n each: sort input, output

@@ -137,6 +137,11 @@ struct TransportLaunch {
 TransportLaunch transport_launch_shape(int n_sm, int threads = 128);
 void launch_transport_history(const MeshDev &m, const CellsDev &c, const Bank &b, DeviceDiag *d,
                               uint32_t seed, const TransportLaunch &shape, cudaStream_t s);
+// history transport of bank entries [first, first + count) with their own
+// work counter (zeroed by the caller)
+void launch_transport_history_range(const MeshDev &m, const CellsDev &c, const Bank &b, DeviceDiag *d,
+                                    uint32_t seed, unsigned long long first, unsigned long long count,
+                                    unsigned long long *queue, const TransportLaunch &shape, cudaStream_t s);
 void launch_census(const Bank &from, const Bank &to, DeviceDiag *d, const unsigned long long *off,
                    double next_dt, int n_sm, cudaStream_t s);
 void launch_transport_resume(const MeshDev &m, const CellsDev &c, const Bank &b, DeviceDiag *d,

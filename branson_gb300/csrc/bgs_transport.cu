@@ -29,11 +29,21 @@ constexpr int min_blocks_for() {
   return (BGS_MIN_BLOCKS * 128 / kThreads) > 0 ? (BGS_MIN_BLOCKS * 128 / kThreads) : 1;
 }
 
+// Work items of one history launch: the whole bank (queue == nullptr: d's
+// bank size and work counter), or bank entries [first, first + count) with
+// their own counter (the pipelined drop-in transports a bank in chunks as
+// its state arrives).
+struct ItemRange {
+  unsigned long long first, count;
+  unsigned long long *queue;
+};
+
 template <bool kResume, int kThreads>
 __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
     k_transport_history(MeshDev m, CellsDev c, Bank b, DeviceDiag *d, unsigned long long seed_hi,
-                        EventState es) {
-  const unsigned long long n = kResume ? (unsigned long long)*es.n_active : d->n_bank;
+                        EventState es, ItemRange rg) {
+  const unsigned long long n = kResume ? (unsigned long long)*es.n_active : (rg.queue ? rg.count : d->n_bank);
+  unsigned long long *const queue = rg.queue ? rg.queue : &d->work_counter;
   const int sa = d->scale_abs, st = d->scale_track;
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lanemask_lt = (1u << lane) - 1u;
@@ -48,12 +58,12 @@ __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
     if (need) {
       const int leader = __ffs(need) - 1;
       unsigned long long base = 0;
-      if ((int)lane == leader) base = atomicAdd(&d->work_counter, (unsigned long long)__popc(need));
+      if ((int)lane == leader) base = atomicAdd(queue, (unsigned long long)__popc(need));
       base = __shfl_sync(0xffffffffu, base, leader);
       if (!active && !done) {
         const unsigned long long w = base + __popc(need & lanemask_lt);
         if (w < n) {
-          const unsigned long long i = kResume ? (unsigned long long)es.active[w] : w;
+          const unsigned long long i = kResume ? (unsigned long long)es.active[w] : rg.first + w;
           L.idx = i;
           L.px = b.px[i]; L.py = b.py[i]; L.pz = b.pz[i];
           L.dx = b.dx[i]; L.dy = b.dy[i]; L.dz = b.dz[i];
@@ -253,30 +263,38 @@ TransportLaunch transport_launch_shape(int n_sm, int threads) {
 
 template <bool kResume>
 void launch_history_kernel(const MeshDev &m, const CellsDev &c, const Bank &b, DeviceDiag *d,
-                           unsigned long long seed_hi, const EventState &es, const TransportLaunch &shape,
-                           cudaStream_t s) {
+                           unsigned long long seed_hi, const EventState &es, const ItemRange &rg,
+                           const TransportLaunch &shape, cudaStream_t s) {
   switch (shape.threads) {
     case 64:
-      k_transport_history<kResume, 64><<<shape.blocks, 64, 0, s>>>(m, c, b, d, seed_hi, es);
+      k_transport_history<kResume, 64><<<shape.blocks, 64, 0, s>>>(m, c, b, d, seed_hi, es, rg);
       break;
     case 256:
-      k_transport_history<kResume, 256><<<shape.blocks, 256, 0, s>>>(m, c, b, d, seed_hi, es);
+      k_transport_history<kResume, 256><<<shape.blocks, 256, 0, s>>>(m, c, b, d, seed_hi, es, rg);
       break;
     default:
-      k_transport_history<kResume, 128><<<shape.blocks, 128, 0, s>>>(m, c, b, d, seed_hi, es);
+      k_transport_history<kResume, 128><<<shape.blocks, 128, 0, s>>>(m, c, b, d, seed_hi, es, rg);
       break;
   }
 }
 
 void launch_transport_history(const MeshDev &m, const CellsDev &c, const Bank &b, DeviceDiag *d,
                               uint32_t seed, const TransportLaunch &shape, cudaStream_t s) {
-  launch_history_kernel<false>(m, c, b, d, (unsigned long long)seed << 32, EventState{}, shape, s);
+  launch_history_kernel<false>(m, c, b, d, (unsigned long long)seed << 32, EventState{}, ItemRange{0, 0, nullptr},
+                               shape, s);
+}
+
+void launch_transport_history_range(const MeshDev &m, const CellsDev &c, const Bank &b, DeviceDiag *d,
+                                    uint32_t seed, unsigned long long first, unsigned long long count,
+                                    unsigned long long *queue, const TransportLaunch &shape, cudaStream_t s) {
+  launch_history_kernel<false>(m, c, b, d, (unsigned long long)seed << 32, EventState{},
+                               ItemRange{first, count, queue}, shape, s);
 }
 
 void launch_transport_resume(const MeshDev &m, const CellsDev &c, const Bank &b, DeviceDiag *d,
                              uint32_t seed, const EventState &es, const TransportLaunch &shape,
                              cudaStream_t s) {
-  launch_history_kernel<true>(m, c, b, d, (unsigned long long)seed << 32, es, shape, s);
+  launch_history_kernel<true>(m, c, b, d, (unsigned long long)seed << 32, es, ItemRange{0, 0, nullptr}, shape, s);
 }
 
 void launch_census(const Bank &from, const Bank &to, DeviceDiag *d, const unsigned long long *off,

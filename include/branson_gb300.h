@@ -334,7 +334,10 @@ enum {
   BGS_OPT_EVENT_TAIL_FRACTION = 2,  /* active share below which event rounds stop */
   BGS_OPT_TRANSPORT_BLOCKS = 3,     /* persistent-grid blocks for the history kernel (0: occupancy);
                                        histories per thread = histories / (blocks * threads) */
-  BGS_OPT_TRANSPORT_THREADS = 4     /* block size of the history kernel: 64, 128 (default) or 256 */
+  BGS_OPT_TRANSPORT_THREADS = 4,    /* block size of the history kernel: 64, 128 (default) or 256 */
+  BGS_OPT_PIPELINE_MIN_PHOTONS = 5  /* bgs_replicated_transport in history mode overlaps its copies
+                                       with chunked transport from this many photons (default 2^20;
+                                       0 never) */
 };
 BGS_API int bgs_set_option(bgs_context *ctx, int option, double value);
 

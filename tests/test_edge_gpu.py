@@ -90,3 +90,32 @@ def test_rare_segment_branches(gpu_lib):
         assert end["descriptor"][1] == 2       # CENSUS
     finally:
         gpu.close()
+
+
+@pytest.mark.parametrize("n", [1, 7, 9, 1031, 20928])
+def test_pipelined_dropin_equals_whole_bank(gpu_lib, n):
+    """The drop-in's pipelined form (copies overlapped with chunked
+    transport, used for large history-mode banks) returns what the one-launch
+    form returns, bit for bit: end states, census, tallies, energies (the
+    threshold is lowered so small lists, including ones that leave some of
+    the eight chunks empty, take the pipelined path)."""
+    import oracle as O
+    from branson_gb300.engine import arrays_to_records, records_to_arrays
+    dk, orc, gpu, photons, nd = _setup()
+    try:
+        outs = []
+        for min_n in (0, 1):  # 0: never pipelined; 1: always
+            gpu.set_option("pipeline_min_photons", min_n)
+            ph = records_to_arrays(photons[:n])
+            abs_g, trk_g, census_g, ce_g, ex_g = gpu.replicated_transport(ph, nd)
+            outs.append((arrays_to_records(ph, O.PHOTON_DTYPE), abs_g, trk_g,
+                         arrays_to_records(census_g, O.PHOTON_DTYPE), ce_g, ex_g))
+        (e0, a0, t0, c0, ce0, ex0), (e1, a1, t1, c1, ce1, ex1) = outs
+        for f in e0.dtype.names:
+            np.testing.assert_array_equal(e1[f], e0[f], err_msg=f"end {f}")
+            np.testing.assert_array_equal(c1[f], c0[f], err_msg=f"census {f}")
+        np.testing.assert_array_equal(a1, a0)
+        np.testing.assert_array_equal(t1, t0)
+        assert (ce1, ex1) == (ce0, ex0)
+    finally:
+        gpu.close()
