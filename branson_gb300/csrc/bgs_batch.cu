@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(kItemThreads) k_batch_items(const ProblemView 
 constexpr bool kBatchFaces = true;
 
 #ifndef BGS_BATCH_MIN_BLOCKS
-#define BGS_BATCH_MIN_BLOCKS 6
+#define BGS_BATCH_MIN_BLOCKS 7
 #endif
 
 __global__ void __launch_bounds__(kTransportThreads, BGS_BATCH_MIN_BLOCKS)
