@@ -180,11 +180,12 @@ __device__ __forceinline__ unsigned long long threefry2x64_20_w0(unsigned long l
 
 // u01fixedpt<double, uint64_t> (RNG.h:202-238): ((w >> 11) | 1) * 2^-53,
 // assembled from integer bits (exact; no floating-point conversion needed).
-__device__ __forceinline__ double u01_from_bits(unsigned long long w) {
+// u * 2^scale (scale 0 or 1: exact) for the draw u = m * 2^-53
+__device__ __forceinline__ double u01_from_bits(unsigned long long w, int scale = 0) {
   const unsigned long long m = (w >> 11) | 1ULL;     // 1 <= m < 2^53, odd
   const int s = __clzll(m) - 11;                     // shift to put the top bit at 52
   const unsigned long long mant = (m << s) & 0x000FFFFFFFFFFFFFULL;
-  const unsigned long long expo = (unsigned long long)(1023 - 1 - s);  // value in [2^-1-s, 2^-s)
+  const unsigned long long expo = (unsigned long long)(1023 - 1 - s + scale);  // u in [2^-1-s, 2^-s)
   return __longlong_as_double((long long)((expo << 52) | mant));
 }
 
@@ -205,6 +206,12 @@ struct Rng {
     const double u = u01_from_bits(threefry2x64_20_w0(ctr, hi, stream));
     ++ctr;
     return u;
+  }
+  // 2u for the next draw u, exactly (the azimuth's u * 2.0)
+  __device__ __forceinline__ double next_twice() {
+    const double u2 = u01_from_bits(threefry2x64_20_w0(ctr, hi, stream), 1);
+    ++ctr;
+    return u2;
   }
   // advance past a draw whose value cannot change the result
   __device__ __forceinline__ void skip() { ++ctr; }

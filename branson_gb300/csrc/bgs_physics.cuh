@@ -174,17 +174,26 @@ __device__ __forceinline__ bool f32_image(double x, float &f) {
   return zero || (mag - (897u << 20)) < ((1151u - 897u) << 20);
 }
 
+// approximate single-precision reciprocal (PTX rcp.approx: within one ulp)
+// of a normal float
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 // The face that get_distance_to_boundary picks (cell.h:117-132), decided
 // from single-precision quotients, with one double division for the
-// winner.  Each approximate quotient is within 2^-20 (relative) of the
-// correctly rounded one (two truncations below 2^-23 and __fdividef's two
-// ulps), so when the winner is separated from every other candidate by
-// more than 2^-18 of their magnitudes, and every quotient from the 1e16
+// winner.  Each approximate quotient (two truncated images, the reciprocal
+// within one ulp, the product) is within 2^-21 (relative) of the correctly
+// rounded one, so when the winner is separated from every other candidate
+// by more than 2^-18 of their magnitudes, and every quotient from the 1e16
 // limit by more than 1e-4 of it, the exact comparisons order them the same
-// way and the division returns the distance the three-division form would.  Anything
-// else (near ties, a zero or subnormal-range direction cosine, a quotient
-// near 1e16 or beyond float's range) returns false and the caller runs the
-// three exact divisions.
+// way and the division returns the distance the three-division form would.
+// Anything else (near ties, a zero or subnormal-range direction cosine, a
+// cosine image whose reciprocal flushes to zero, a quotient near 1e16 or
+// beyond float's range) returns false and the caller runs the three exact
+// divisions.
 __device__ __forceinline__ bool approx_faces(double ax, double ay, double az, const Lane &L, bool posx,
                                              bool posy, bool posz, double &dist_to_boundary,
                                              long long &k_boundary, uint32_t &surface_cross) {
@@ -192,7 +201,11 @@ __device__ __forceinline__ bool approx_faces(double ax, double ay, double az, co
   bool ok = f32_image(ax, fax) & f32_image(ay, fay) & f32_image(az, faz);
   ok &= f32_image(L.dx, fdx) & f32_image(L.dy, fdy) & f32_image(L.dz, fdz);
   ok &= (fdx != 0.0f) & (fdy != 0.0f) & (fdz != 0.0f);
-  const float qx = __fdividef(fax, fdx), qy = __fdividef(fay, fdy), qz = __fdividef(faz, fdz);
+  const float rx = rcp_approx(fdx), ry = rcp_approx(fdy), rz = rcp_approx(fdz);
+  // reciprocals that flushed to zero (cosine images above 2^126) fall back
+  ok &= ((__float_as_uint(rx) & 0x7F800000u) != 0) & ((__float_as_uint(ry) & 0x7F800000u) != 0) &
+        ((__float_as_uint(rz) & 0x7F800000u) != 0);
+  const float qx = fax * rx, qy = fay * ry, qz = faz * rz;
   constexpr float kLo = 9.9999e15f, kHi = 1.0001e16f, kTol = 3.814697265625e-06f;  // 1e16 -+ 1e-4, 2^-18
   const float kInf = __int_as_float(0x7f800000);
   ok &= !(qx >= kLo && qx <= kHi) & !(qy >= kLo && qy <= kHi) & !(qz >= kLo && qz <= kHi);
@@ -315,7 +328,7 @@ template <bool kFaces = false>
 __device__ __forceinline__ void scatter_update(const MeshDev &m, const CellsDev &c, const CellXS &xs,
                                                Lane &L) {
   const double mu = mu_from_m53(L.rng.next_m53());
-  const double phi = L.rng.next() * 2.0 * kPi;
+  const double phi = L.rng.next_twice() * kPi;  // RN(RN(u * 2.0) * pi), u * 2.0 exact
   const double sin_theta = fix::sqrt_rn(1.0 - mu * mu);
   double sp, cp;
   fix::sincos_phi(phi, &sp, &cp);

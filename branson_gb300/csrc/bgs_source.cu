@@ -50,7 +50,7 @@ __device__ __forceinline__ void position_in_cell(const double n[6], Rng &r, doub
 // get_uniform_angle (sampling_functions.h:57-70)
 __device__ __forceinline__ void uniform_angle(Rng &r, double d[3]) {
   const double mu = mu_from_m53(r.next_m53());
-  const double phi = r.next() * 2.0 * kPi;
+  const double phi = r.next_twice() * kPi;  // RN(RN(u * 2.0) * pi), u * 2.0 exact
   const double sin_theta = sqrt(1.0 - mu * mu);
   double s, c;
   fix::sincos_phi(phi, &s, &c);
@@ -84,7 +84,7 @@ __device__ __forceinline__ void source_angle(Rng &r, int face, double d[3]) {
   const double u = r.next();
   const double ct = sqrt(u);
   const double st = sqrt(1.0 - u);
-  const double phi = r.next() * 2.0 * kPi;
+  const double phi = r.next_twice() * kPi;  // RN(RN(u * 2.0) * pi), u * 2.0 exact
   const double sign = (face % 2) ? -1.0 : 1.0;
   double sp, cp;
   fix::sincos_phi(phi, &sp, &cp);

@@ -29,6 +29,20 @@ def _uniform_deck():
                 regions=[Region(1, 0.1, 1.0, 10.0, 0.0, 0.0, 0.0, 0.5, 0.0)])
 
 
+def _offset_scatter_deck():
+    """Collision-dominated cells on an offset mesh whose z planes straddle 0
+    (x in [-7.5, -7.3], y in [2, 2.12], z in [-0.05, 0.05]), physical and
+    effective scattering, reflecting and vacuum faces, two groups: long
+    runs of collisions inside a cell, ending near its faces, on planes of
+    both signs and magnitudes from 0 to 7.5."""
+    from branson_gb300.deck import Deck, Division, Region, REFLECT, VACUUM
+    return Deck(t_start=0.0, t_stop=0.03, dt_start=0.01, t_mult=1.0, dt_max=1.0, photons=20000, seed=5,
+                x_divisions=[Division(-7.5, -7.3, 6)], y_divisions=[Division(2.0, 2.12, 4)],
+                z_divisions=[Division(-0.05, 0.05, 5)], region_map={(0, 0, 0): 1},
+                bc=(REFLECT, VACUUM, REFLECT, VACUUM, REFLECT, VACUUM), T_source=0.0, n_groups=2,
+                regions=[Region(1, 0.1, 1.0, 300.0, 0.0, 0.0, 500.0, 0.3, 0.3)])
+
+
 def _decks():
     from branson_gb300 import deck as D
     return {
@@ -36,6 +50,7 @@ def _decks():
         "hot_zone": D.hot_zone(n_per_axis=10, photons=20000, n_steps=3),
         "hohlraum30": D.hohlraum(n_per_axis=10, photons=20000, n_steps=2, n_groups=30),
         "uniform8": _uniform_deck(),
+        "offset_scatter": _offset_scatter_deck(),
     }
 
 
@@ -44,7 +59,7 @@ def _extent(dk):
     return max(x[-1] - x[0], y[-1] - y[0], z[-1] - z[0], C_LIGHT * dk.dt_start)
 
 
-@pytest.mark.parametrize("name", ["marshak", "hot_zone", "hohlraum30"])
+@pytest.mark.parametrize("name", ["marshak", "hot_zone", "hohlraum30", "offset_scatter"])
 def test_dropin_transport_matches_oracle(gpu_lib, name):
     import oracle as O
     from branson_gb300.engine import ReplicatedIMC, arrays_to_records, records_to_arrays
@@ -85,7 +100,7 @@ def test_dropin_transport_matches_oracle(gpu_lib, name):
         gpu.close()
 
 
-@pytest.mark.parametrize("name", ["marshak", "hot_zone", "hohlraum30", "uniform8"])
+@pytest.mark.parametrize("name", ["marshak", "hot_zone", "hohlraum30", "uniform8", "offset_scatter"])
 def test_device_step_matches_oracle(gpu_lib, name):
     import oracle as O
     from branson_gb300.engine import ReplicatedIMC, arrays_to_records
