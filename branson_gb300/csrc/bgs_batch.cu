@@ -77,6 +77,18 @@ constexpr bool kBatchFaces = true;
 #define BGS_BATCH_MIN_BLOCKS 7
 #endif
 
+// flush visits taken from the ring, each into its own problem's tallies
+// with that problem's scales; range flags go to that problem
+__device__ __forceinline__ void flush_ring_batched(const ProblemView *__restrict__ probs, bool take,
+                                                   unsigned long long key, double a, double t) {
+  const uint32_t q = (uint32_t)(key >> 32), cell = (uint32_t)key;
+  TallyCell *tally = take ? probs[q].c.tally : nullptr;
+  const int sa = take ? probs[q].d->scale_abs : 0, st = take ? probs[q].d->scale_track : 0;
+  uint32_t f = 0;
+  flush_tally_warp(tally, take, key, cell, a, t, f, sa, st);
+  if (f) atomicOr(&probs[q].d->flags, f);
+}
+
 __global__ void __launch_bounds__(kTransportThreads, BGS_BATCH_MIN_BLOCKS)
     k_transport_batched(const ProblemView *__restrict__ probs, uint32_t n_probs,
                         const unsigned long long *__restrict__ item_off, unsigned long long *work_counter) {
@@ -89,6 +101,9 @@ __global__ void __launch_bounds__(kTransportThreads, BGS_BATCH_MIN_BLOCKS)
   uint32_t p = 0;
   const CellXS *xs_p = nullptr;
   bool active = false, done = false;
+  __shared__ FlushRing rings[kTransportThreads / 32];
+  FlushRing &ring = rings[threadIdx.x >> 5];
+  uint32_t head = 0, tail = 0;  // the warp's ring counters (the same in every lane)
 
   while (true) {
     const unsigned need = __ballot_sync(0xffffffffu, !active && !done);
@@ -134,8 +149,9 @@ __global__ void __launch_bounds__(kTransportThreads, BGS_BATCH_MIN_BLOCKS)
     if (__all_sync(0xffffffffu, !active)) break;
 
     // ---- one segment of transport_photon (history_based_transport.h:55-139);
-    // flushes go through one warp-wide aggregated flush keyed on
-    // (problem, cell), as in k_transport_history
+    // ended cell visits wait in the warp's ring and go, 32 at a time,
+    // through one warp-wide aggregated flush keyed on (problem, cell), as in
+    // k_transport_history
     bool flush = false, ended = false;
     uint32_t fcell = 0;
     double fa = 0.0, ft = 0.0;
@@ -168,19 +184,31 @@ __global__ void __launch_bounds__(kTransportThreads, BGS_BATCH_MIN_BLOCKS)
         }
       }
     }
-    {
+    ring_push(ring, tail, tail, flush, ((unsigned long long)p << 32) | fcell, fa, ft);
+    if (ended) {
       const ProblemView &P = probs[p];
-      const int sa = flush ? P.d->scale_abs : 0, st = flush ? P.d->scale_track : 0;
-      flush_tally_warp(P.c.tally, flush, ((unsigned long long)p << 32) | fcell, fcell, fa, ft, flags, sa, st);
-      if (ended) {
-        atomicAdd(&P.d->n_segments, (unsigned long long)L.segs);
-        if (flags) {
-          atomicOr(&P.d->flags, flags);
-          flags = 0;
-        }
-        active = false;
+      atomicAdd(&P.d->n_segments, (unsigned long long)L.segs);
+      if (flags) {
+        atomicOr(&P.d->flags, flags);
+        flags = 0;
       }
+      active = false;
     }
+    if (tail - head >= 32u) {
+      unsigned long long key;
+      double a, t;
+      ring_take(ring, head, 32u, key, a, t);
+      flush_ring_batched(probs, true, key, a, t);
+      head += 32u;
+    }
+  }
+  while (tail != head) {  // the visits still waiting
+    const uint32_t k = min(tail - head, 32u);
+    unsigned long long key;
+    double a, t;
+    const bool take = ring_take(ring, head, k, key, a, t);
+    flush_ring_batched(probs, take, key, a, t);
+    head += k;
   }
   __syncthreads();
   if (threadIdx.x == 0) atomicMax(&work_counter[2], global_ns());

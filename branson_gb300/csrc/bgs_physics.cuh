@@ -111,6 +111,47 @@ __device__ __forceinline__ void flush_tally_warp(TallyCell *tally, bool flush, K
 }
 
 
+// Per-warp ring of cell visits waiting for their tally flush, in shared
+// memory.  A loop trip ends a visit in only a few lanes, so flushing every
+// trip runs the conversions, the cell match and the atomics (whose L2
+// round trip the warp waits for) with most lanes idle; instead each trip
+// appends its ended visits, and once 32 are waiting the whole warp flushes
+// them, one visit per lane.  Integer tally sums do not depend on the order
+// of the adds, so the tallies are the same bits.  key is the cell, or
+// problem << 32 | cell in the batched kernel.
+constexpr uint32_t kFlushRing = 64;  // < 32 waiting before a trip's (at most 32) appends
+struct FlushRing {
+  unsigned long long key[kFlushRing];
+  double a[kFlushRing], t[kFlushRing];
+};
+
+// append this trip's ended visits; head/tail are the warp's (uniform) counters
+__device__ __forceinline__ void ring_push(FlushRing &r, uint32_t tail_in, uint32_t &tail, bool flush,
+                                          unsigned long long key, double a, double t) {
+  const unsigned fb = __ballot_sync(0xffffffffu, flush);
+  if (flush) {
+    const uint32_t s = (tail_in + __popc(fb & ((1u << (threadIdx.x & 31u)) - 1u))) & (kFlushRing - 1u);
+    r.key[s] = key;
+    r.a[s] = a;
+    r.t[s] = t;
+  }
+  tail = tail_in + __popc(fb);
+}
+
+// take the next n (<= 32) waiting visits, one per lane (flush false past n)
+__device__ __forceinline__ bool ring_take(const FlushRing &r, uint32_t head, uint32_t n, unsigned long long &key,
+                                          double &a, double &t) {
+  __syncwarp();
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t s = (head + lane) & (kFlushRing - 1u);
+  const bool take = lane < n;
+  key = take ? r.key[s] : 0ULL;
+  a = take ? r.a[s] : 0.0;
+  t = take ? r.t[s] : 0.0;
+  __syncwarp();  // every lane has read its slot before the slots are reused
+  return take;
+}
+
 __device__ __forceinline__ void store_end(const Bank &b, const Lane &L, uint8_t desc) {
   const unsigned long long i = L.idx;
   b.px[i] = L.px; b.py[i] = L.py; b.pz[i] = L.pz;
@@ -360,7 +401,17 @@ __device__ __forceinline__ int face_bc(const MeshDev &m, const Lane &L, uint32_t
     case 4: interior = L.ck > 0; break;
     default: interior = L.ck + 1 < m.ngz; break;
   }
-  return interior ? ELEMENT : m.bc[surface_cross];
+  if (interior) return ELEMENT;
+  // constant indices: a variable index into the kernel parameter's array
+  // would make the compiler copy the whole MeshDev to local memory
+  switch (surface_cross) {
+    case 0: return m.bc[0];
+    case 1: return m.bc[1];
+    case 2: return m.bc[2];
+    case 3: return m.bc[3];
+    case 4: return m.bc[4];
+    default: return m.bc[5];
+  }
 }
 
 // ELEMENT crossing: the photon enters the neighbour (cell.h:110-112); only

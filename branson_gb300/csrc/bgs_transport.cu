@@ -51,6 +51,9 @@ __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
   unsigned long long seg_total = 0;
   Lane L;
   bool active = false, done = false;
+  __shared__ FlushRing rings[kThreads / 32];
+  FlushRing &ring = rings[threadIdx.x >> 5];
+  uint32_t head = 0, tail = 0;  // the warp's ring counters (the same in every lane)
 
   while (true) {
     // ---- refill lanes whose history ended
@@ -92,9 +95,8 @@ __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
     if (__all_sync(0xffffffffu, !active)) break;
 
     // ---- one segment of transport_photon (history_based_transport.h:55-139);
-    // every flush of the loop trip goes through one warp-wide aggregated
-    // flush after the event handling (lanes without a history take part
-    // with nothing to add)
+    // ended cell visits wait in the warp's ring, and every 32 of them go
+    // through one warp-wide aggregated flush (FlushRing)
     bool flush = false;
     uint32_t fcell = 0;
     double fa = 0.0, ft = 0.0;
@@ -131,7 +133,22 @@ __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
         }
       }
     }
-    flush_tally_warp(c.tally, flush, fcell, fcell, fa, ft, flags, sa, st);
+    ring_push(ring, tail, tail, flush, fcell, fa, ft);
+    if (tail - head >= 32u) {
+      unsigned long long key;
+      double a, t;
+      ring_take(ring, head, 32u, key, a, t);
+      flush_tally_warp(c.tally, true, (uint32_t)key, (uint32_t)key, a, t, flags, sa, st);
+      head += 32u;
+    }
+  }
+  while (tail != head) {  // the visits still waiting
+    const uint32_t k = min(tail - head, 32u);
+    unsigned long long key;
+    double a, t;
+    const bool take = ring_take(ring, head, k, key, a, t);
+    flush_tally_warp(c.tally, take, (uint32_t)key, (uint32_t)key, a, t, flags, sa, st);
+    head += k;
   }
 
   // ---- per-warp totals
