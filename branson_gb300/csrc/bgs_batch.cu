@@ -78,14 +78,14 @@ constexpr bool kBatchFaces = true;
 #endif
 
 // flush visits taken from the ring, each into its own problem's tallies
-// with that problem's scales; range flags go to that problem
+// with that problem's scale; range flags go to that problem
 __device__ __forceinline__ void flush_ring_batched(const ProblemView *__restrict__ probs, bool take,
                                                    unsigned long long key, double a, double t) {
   const uint32_t q = (uint32_t)(key >> 32), cell = (uint32_t)key;
   TallyCell *tally = take ? probs[q].c.tally : nullptr;
-  const int sa = take ? probs[q].d->scale_abs : 0, st = take ? probs[q].d->scale_track : 0;
+  const int sa = take ? probs[q].d->scale_abs : 0;
   uint32_t f = 0;
-  flush_tally_warp(tally, take, key, cell, a, t, f, sa, st);
+  flush_tally_warp(tally, take, key, cell, a, t, f, sa);
   if (f) atomicOr(&probs[q].d->flags, f);
 }
 
@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(kTransportThreads, BGS_BATCH_MIN_BLOCKS)
           flush = true;
           fcell = L.cell;
           fa = L.thr_abs;
-          ft = visit_track(xs, L, ev);
+          ft = visit_deposit(L, ev);
         }
         if (ev == SEG_KILLED || ev == SEG_CENSUS || bc == VACUUM || bc == SOURCE || bc == PROCESSOR) {
           const uint8_t desc = ev == SEG_KILLED ? KILLED

@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(kEventThreads) k_event_advance(MeshDev m, Cell
                                                                 DeviceDiag *d, unsigned long long seed_hi,
                                                                 EventState es, bool first) {
   const unsigned int n = *es.n_active;
-  const int sa = d->scale_abs, st = d->scale_track;
+  const int sa = d->scale_abs;
   uint32_t flags = 0;
   unsigned long long segs = 0;
   // uniform trip count per warp so the queue ballots see every lane
@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(kEventThreads) k_event_advance(MeshDev m, Cell
           flush = true;
           fcell = L.cell;
           fa = L.thr_abs;
-          ft = visit_track(xs, L, ev);
+          ft = visit_deposit(L, ev);
           store_end(b, L, ev == SEG_KILLED ? KILLED : CENSUS);
         } else {
           b.px[p] = L.px; b.py[p] = L.py; b.pz[p] = L.pz;
@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(kEventThreads) k_event_advance(MeshDev m, Cell
         }
       }
     }
-    flush_tally_warp(c.tally, flush, fcell, fcell, fa, ft, flags, sa, st);
+    flush_tally_warp(c.tally, flush, fcell, fcell, fa, ft, flags, sa);
     queue_push(ev == SEG_SCATTER, p, es.q_scatter, es.n_scatter);
     queue_push(ev == SEG_BOUNDARY, p, es.q_boundary, es.n_boundary);
   }
@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(kEventThreads) k_event_scatter(MeshDev m, Cell
 __global__ void __launch_bounds__(kEventThreads) k_event_boundary(MeshDev m, CellsDev c, Bank b,
                                                                  DeviceDiag *d, EventState es) {
   const unsigned int n = *es.n_boundary;
-  const int sa = d->scale_abs, st = d->scale_track;
+  const int sa = d->scale_abs;
   uint32_t flags = 0;
   const unsigned int stride = gridDim.x * blockDim.x;
   const unsigned int warp_base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(kEventThreads) k_event_boundary(MeshDev m, Cel
         survive = true;
       }
     }
-    flush_tally_warp(c.tally, flush, fcell, fcell, fa, flush ? fa * c.xs[fcell].inv_saf : 0.0, flags, sa, st);
+    flush_tally_warp(c.tally, flush, fcell, fcell, fa, 0.0, flags, sa);
     queue_push(survive, p, es.next, es.n_next);
   }
   for (int o = 16; o > 0; o >>= 1) flags |= __shfl_down_sync(0xffffffffu, flags, o);

@@ -6,8 +6,9 @@
 //   cells    : structure of arrays of doubles, one entry per cell
 //              (T_e, T_r initial, T_s, op_a, op_s, f, emission/census/source E,
 //              T_r diagnostic) plus the transport table XS[n] (32 B per cell)
-//   tallies  : TallyCell[n] = 128-bit fixed-point absorbed and track energy
-//              (32 B per cell), order-independent integer sums
+//   tallies  : TallyCell[n] = 128-bit fixed-point absorbed energy and its
+//              cutoff-kill part (32 B per cell), order-independent integer
+//              sums; the track tally is formed from them per cell
 //   photons  : two banks, each a structure of arrays sized to the capacity
 //   counts   : per-cell photon counts and their exclusive prefix sums
 //   diag     : one DeviceDiag (step scalars, flags)
@@ -58,9 +59,15 @@ struct __align__(16) CellXS {
   double sig_eff, neg_saf, inv_saf, p_scat, inv_se;
 };
 
-// 128-bit fixed-point tally cell: value = (hi*2^64 + lo) * 2^-scale.
+// 128-bit fixed-point tally cell: value = (hi*2^64 + lo) * 2^-scale_abs.
+// abs is the absorbed energy (Cell_Tally::abs_E); dep is the part of it
+// deposited by cutoff kills.  The track-length tally is formed per cell
+// from the two: track_E = (abs - dep) / (sigma_a f), since sigma_a f is
+// constant in a cell over a step and a kill deposit adds to abs_E only
+// (history_based_transport.h:74-82); so a visit flushes one tally, and a
+// kill a second one.
 struct __align__(32) TallyCell {
-  unsigned long long abs_lo, abs_hi, trk_lo, trk_hi;
+  unsigned long long abs_lo, abs_hi, dep_lo, dep_hi;
 };
 
 // Photon bank: structure of arrays (photon.h:172-181 fields).
@@ -145,7 +152,7 @@ struct DeviceDiag {
   unsigned long long census_counter;  // (unused by the scan path)
   unsigned long long sum_census[2], sum_exit[2], sum_abs[2];  // 128-bit fixed point
   double census_E, exit_E, absorbed_E, post_mat_E;
-  int scale_abs, scale_track;         // fixed-point exponents of this step
+  int scale_abs;                      // fixed-point exponent of this step's energy sums
   uint32_t flags;
   uint32_t serial_needed;             // a photon count needed the serial energy sum
 };

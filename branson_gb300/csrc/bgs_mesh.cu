@@ -368,27 +368,18 @@ __global__ void k_scan_add(unsigned long long *out, uint32_t n, const unsigned l
 }
 
 // ---------------------------------------------------------------------------
-// Fixed-point scales for a bank of photons: bounds from the largest photon
-// energy and the longest remaining flight (order-independent maxima, so the
-// scales and hence the tallies are deterministic).
+// Fixed-point scale for a bank of photons: the bound from the largest photon
+// energy (an order-independent maximum, so the scale and hence the tallies
+// are deterministic).
 __device__ __forceinline__ void bank_bounds_body(const Bank &b, const DeviceDiag *d, unsigned long long *max_bits,
                                                  uint32_t bx, uint32_t nbx) {
   const unsigned long long n = d->n_bank;
-  unsigned long long mE = 0, mL = 0;
+  unsigned long long mE = 0;
   for (unsigned long long i = bx * (unsigned long long)blockDim.x + threadIdx.x; i < n;
-       i += (unsigned long long)nbx * blockDim.x) {
-    const double e = fabs(b.E[i]), l = fabs(b.life[i]);
-    mE = max(mE, (unsigned long long)__double_as_longlong(e));
-    mL = max(mL, (unsigned long long)__double_as_longlong(l));
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    mE = max(mE, __shfl_down_sync(0xffffffffu, mE, o));
-    mL = max(mL, __shfl_down_sync(0xffffffffu, mL, o));
-  }
-  if ((threadIdx.x & 31) == 0) {
-    atomicMax(&max_bits[0], mE);
-    atomicMax(&max_bits[1], mL);
-  }
+       i += (unsigned long long)nbx * blockDim.x)
+    mE = max(mE, (unsigned long long)__double_as_longlong(fabs(b.E[i])));
+  for (int o = 16; o > 0; o >>= 1) mE = max(mE, __shfl_down_sync(0xffffffffu, mE, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(&max_bits[0], mE);
 }
 
 __global__ void k_bank_bounds(Bank b, const DeviceDiag *d, unsigned long long *max_bits) {
@@ -397,14 +388,11 @@ __global__ void k_bank_bounds(Bank b, const DeviceDiag *d, unsigned long long *m
 
 __device__ __forceinline__ void set_scales_body(DeviceDiag *d, const unsigned long long *max_bits) {
   const double maxE = __longlong_as_double((long long)max_bits[0]);
-  const double maxL = __longlong_as_double((long long)max_bits[1]);
   const double n = (double)(d->n_bank > 0 ? d->n_bank : 1ULL);
-  // absorbed energy of a history <= its starting energy; its track-length
-  // tally <= starting energy * remaining flight (transport_photon :74-79)
+  // absorbed energy of a history (and any of its parts) <= its starting
+  // energy (transport_photon :74-82)
   const double bound_abs = 2.0 * maxE * n + 1e-300;
-  const double bound_trk = 2.0 * maxE * fmax(maxL, 1e-300) * n + 1e-300;
   d->scale_abs = fixed_scale_for(bound_abs);
-  d->scale_track = fixed_scale_for(bound_trk);
 }
 
 __global__ void k_set_scales(DeviceDiag *d, const unsigned long long *max_bits) { set_scales_body(d, max_bits); }
@@ -478,7 +466,11 @@ __device__ __forceinline__ void tally_to_double_body(const MeshDev &m, const Cel
     if (g < m.n_cells) {
       const TallyCell t = c.tally[g];
       abs_out[g] = from_fixed128(t.abs_lo, t.abs_hi, d->scale_abs);
-      track_out[g] = from_fixed128(t.trk_lo, t.trk_hi, d->scale_track);
+      // track_E = (abs - dep) / (sigma_a f), by the cell's RN(1/(sigma_a f));
+      // a cell that absorbed nothing has none (TallyCell)
+      const unsigned long long vlo = t.abs_lo - t.dep_lo;
+      const unsigned long long vhi = t.abs_hi - t.dep_hi - (t.abs_lo < t.dep_lo ? 1ULL : 0ULL);
+      track_out[g] = (vlo | vhi) ? from_fixed128(vlo, vhi, d->scale_abs) * c.xs[g].inv_saf : 0.0;
       alo = t.abs_lo;
       ahi = t.abs_hi;
     }

@@ -41,7 +41,7 @@ struct Lane {
   double kill_thr;  // RN(0.01 * E0): the cutoff test runs against it in integer ulps
   double fx, fy, fz;  // the current cell's face planes ahead along x, y, z (kFaces)
   double thr_abs;   // absorbed energy of the current cell visit
-  double thr_trk;   // the visit's track tally, set by a cutoff kill (visit_track)
+  double thr_dep;   // the remaining energy a cutoff kill deposits (visit_deposit)
   unsigned long long idx;
   Rng rng;
   uint32_t cell, group, ci, cj, ck, segs;
@@ -77,7 +77,7 @@ __device__ __forceinline__ void add128(unsigned long long &lo, unsigned long lon
 
 template <typename Key>
 __device__ __forceinline__ void flush_tally_warp(TallyCell *tally, bool flush, Key key, uint32_t cell, double a,
-                                                 double t, uint32_t &flags, int sa, int st) {
+                                                 double t, uint32_t &flags, int sa) {
   if (!__any_sync(0xffffffffu, flush)) return;
   unsigned long long alo = 0, ahi = 0, tlo = 0, thi = 0;
   if (flush) {
@@ -85,7 +85,7 @@ __device__ __forceinline__ void flush_tally_warp(TallyCell *tally, bool flush, K
       flags |= (a == a) ? FLAG_TALLY_RANGE : FLAG_NAN;
       alo = ahi = 0;
     }
-    if ((__double_as_longlong(t) << 1) != 0 && !to_fixed128(t, st, tlo, thi)) {
+    if ((__double_as_longlong(t) << 1) != 0 && !to_fixed128(t, sa, tlo, thi)) {
       flags |= (t == t) ? FLAG_TALLY_RANGE : FLAG_NAN;
       tlo = thi = 0;
     }
@@ -106,7 +106,7 @@ __device__ __forceinline__ void flush_tally_warp(TallyCell *tally, bool flush, K
   if ((int)(threadIdx.x & 31u) == __ffs(grp) - 1) {
     TallyCell *tc = &tally[cell];
     if (alo | ahi) atomic_add128(&tc->abs_lo, &tc->abs_hi, alo, ahi);
-    if (tlo | thi) atomic_add128(&tc->trk_lo, &tc->trk_hi, tlo, thi);
+    if (tlo | thi) atomic_add128(&tc->dep_lo, &tc->dep_hi, tlo, thi);
   }
 }
 
@@ -192,13 +192,14 @@ __device__ __forceinline__ bool f64_positive(double x) { return __double_as_long
 // what one segment ends in (the event branches of transport_photon)
 enum SegEvent : int { SEG_KILLED = 0, SEG_SCATTER = 1, SEG_BOUNDARY = 2, SEG_CENSUS = 3 };
 
-// Track-length tally of the cell visit being flushed.  Upstream adds
-// absorbed/(sigma_a f) per segment (history_based_transport.h:75-77); sigma_a
-// f is constant within a visit, so it is formed once per visit from the
-// visit's absorbed sum (equal up to rounding).  A cutoff kill forms it
-// before the remaining weight is deposited (segment_advance).
-__device__ __forceinline__ double visit_track(const CellXS &xs, const Lane &L, int ev) {
-  return ev == SEG_KILLED ? L.thr_trk : L.thr_abs * xs.inv_saf;
+// Cutoff-kill part of the absorbed energy of the visit being flushed (the
+// remaining weight a killed history deposits, history_based_transport.h:
+// 81-82); the track-length tally of a cell is (abs - dep) / (sigma_a f)
+// (TallyCell).  Upstream adds absorbed/(sigma_a f) per segment
+// (history_based_transport.h:75-77); with sigma_a f constant in the cell
+// over the step, the per-cell form is equal up to rounding.
+__device__ __forceinline__ double visit_deposit(const Lane &L, int ev) {
+  return ev == SEG_KILLED ? L.thr_dep : 0.0;
 }
 
 // Single-precision image of a double, truncated (relative error below
@@ -353,7 +354,7 @@ __device__ __forceinline__ int segment_advance(const MeshDev &m, const double *E
   if (k_e - k_thr <= 4 && k_thr - k_e <= 4) killed = L.E / E0s[L.idx] < kCutoff;
   if (killed || L.segs >= kMaxSegmentsPerHistory) {
     if (!killed) flags |= FLAG_SEGMENT_LIMIT;
-    L.thr_trk = L.thr_abs * xs.inv_saf;  // the visit's track tally, before the kill deposit
+    L.thr_dep = L.E;  // the kill deposit, outside the track tally
     L.thr_abs += L.E;
     return SEG_KILLED;
   }

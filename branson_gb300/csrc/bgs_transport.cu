@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
                         EventState es, ItemRange rg) {
   const unsigned long long n = kResume ? (unsigned long long)*es.n_active : (rg.queue ? rg.count : d->n_bank);
   unsigned long long *const queue = rg.queue ? rg.queue : &d->work_counter;
-  const int sa = d->scale_abs, st = d->scale_track;
+  const int sa = d->scale_abs;
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lanemask_lt = (1u << lane) - 1u;
   uint32_t flags = 0;
@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
           flush = true;
           fcell = L.cell;
           fa = L.thr_abs;
-          ft = visit_track(xs, L, ev);
+          ft = visit_deposit(L, ev);
         }
         if (ev == SEG_KILLED) {
           store_end(b, L, KILLED);
@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
       unsigned long long key;
       double a, t;
       ring_take(ring, head, 32u, key, a, t);
-      flush_tally_warp(c.tally, true, (uint32_t)key, (uint32_t)key, a, t, flags, sa, st);
+      flush_tally_warp(c.tally, true, (uint32_t)key, (uint32_t)key, a, t, flags, sa);
       head += 32u;
     }
   }
@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
     unsigned long long key;
     double a, t;
     const bool take = ring_take(ring, head, k, key, a, t);
-    flush_tally_warp(c.tally, take, (uint32_t)key, (uint32_t)key, a, t, flags, sa, st);
+    flush_tally_warp(c.tally, take, (uint32_t)key, (uint32_t)key, a, t, flags, sa);
     head += k;
   }
 
