@@ -38,6 +38,16 @@ struct ItemRange {
   unsigned long long *queue;
 };
 
+// a lane's segment count, in 32 bits (one register): an ended history adds
+// at most 1e8, and the count goes to the launch total before it reaches 2^31
+__device__ __forceinline__ void add_segments(uint32_t &total, uint32_t segs, DeviceDiag *d) {
+  total += segs;
+  if (total >= (1u << 31)) {
+    atomicAdd(&d->n_segments, (unsigned long long)total);
+    total = 0;
+  }
+}
+
 template <bool kResume, int kThreads>
 __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
     k_transport_history(MeshDev m, CellsDev c, Bank b, DeviceDiag *d, unsigned long long seed_hi,
@@ -48,7 +58,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lanemask_lt = (1u << lane) - 1u;
   uint32_t flags = 0;
-  unsigned long long seg_total = 0;
+  uint32_t seg_total = 0;  // segments of this lane's ended histories (kept below 2^31)
   Lane L;
   bool active = false, done = false;
   __shared__ FlushRing rings[kThreads / 32];
@@ -101,7 +111,6 @@ __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
     uint32_t fcell = 0;
     double fa = 0.0, ft = 0.0;
     if (active) {
-      ++seg_total;
       const CellXS xs = c.xs[L.cell];
       uint32_t surface_cross;
       const int ev = segment_advance(m, b.E0, xs, L, surface_cross, flags);
@@ -119,15 +128,18 @@ __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
         if (ev == SEG_KILLED) {
           store_end(b, L, KILLED);
           active = false;
+          add_segments(seg_total, L.segs, d);
         } else if (ev == SEG_CENSUS) {
           store_end(b, L, CENSUS);
           active = false;
+          add_segments(seg_total, L.segs, d);
         } else if (bc == ELEMENT) {
           L.thr_abs = 0.0;
           enter_neighbour(m, L, surface_cross);
         } else if (bc == VACUUM || bc == SOURCE || bc == PROCESSOR) {
           store_end(b, L, bc == PROCESSOR ? PASS : EXIT);
           active = false;
+          add_segments(seg_total, L.segs, d);
         } else {
           reflect(m, L, surface_cross);
         }
@@ -152,12 +164,13 @@ __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
   }
 
   // ---- per-warp totals
+  unsigned long long segs = seg_total;
   for (int o = 16; o > 0; o >>= 1) {
-    seg_total += __shfl_down_sync(0xffffffffu, seg_total, o);
+    segs += __shfl_down_sync(0xffffffffu, segs, o);
     flags |= __shfl_down_sync(0xffffffffu, flags, o);
   }
   if (lane == 0) {
-    atomicAdd(&d->n_segments, seg_total);
+    atomicAdd(&d->n_segments, segs);
     if (flags) atomicOr(&d->flags, flags);
   }
 }
