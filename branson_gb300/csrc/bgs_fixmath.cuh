@@ -18,7 +18,8 @@
 //        tau = (32*q + j) ln2/1024 + s, exp(-tau) = 2^-q 2^(-j/1024) e^(-s),
 //        e^(-s) by its Taylor series.
 //   sin/cos: Cody-Waite style reduction by pi/2 with a 128-bit 2/pi, octant
-//        symmetry, Taylor series on [0, pi/4].
+//        symmetry, minimax polynomials on [0, pi/4] (Remez exchange, in
+//        gen_fixmath_tables.py).
 // Tables (bgs_fixmath_tables.h) are generated from Python's decimal module.
 // The same source compiles for the host (tests compare it against quad
 // precision and glibc) and for the device.
@@ -262,7 +263,7 @@ BGS_HD double exp_neg(double tau) {
 // (get_uniform_angle, sampling_functions.h:63-67).  phi * 2/pi is formed
 // exactly enough in Q124 (128-bit constant), the quadrant and octant are
 // taken off by symmetry, and sin/cos of the remaining angle in [0, pi/4] are
-// Taylor polynomials in fixed point; the small one of the pair is always a
+// polynomials in fixed point; the small one of the pair is always a
 // sine computed relative to its argument, so tiny results keep full
 // precision.  Results are rounded to nearest.
 struct SinCos {
@@ -270,8 +271,8 @@ struct SinCos {
 };
 
 BGS_HD SinCos sincos_phi_v(double phi) {
-  constexpr uint64_t kS[10] = {BGS_SIN_COEF_INIT};
-  constexpr uint64_t kCo[10] = {BGS_COS_COEF_INIT};
+  constexpr uint64_t kS[fixtab::kSinTerms] = {BGS_SIN_COEF_INIT};
+  constexpr uint64_t kCo[fixtab::kCosTerms] = {BGS_COS_COEF_INIT};
   const uint64_t pb = double_to_bits(phi);
   const int be = (int)((pb >> 52) & 0x7FF);
   // 0 < phi < 8 by the bit pattern (8.0 is 0x4020000000000000; a set sign
@@ -324,15 +325,15 @@ BGS_HD SinCos sincos_phi_v(double phi) {
     const uint64_t Tm = mulhi(Xn, fixtab::kPiOver2_q62);     // theta = Tm * 2^(-58-lz)
     const uint64_t th64 = lz >= 6 ? (lz - 6 >= 64 ? 0 : Tm >> (lz - 6)) : Tm << (6 - lz);  // theta * 2^64
     const uint64_t y = mulhi(th64, th64);                    // theta^2 * 2^64
-    uint64_t b = kS[9];
+    uint64_t b = kS[fixtab::kSinTerms - 1];
 #pragma unroll
-    for (int k = 8; k >= 0; --k) b = kS[k] - mulhi(y, b);   // 1/3! - y(1/5! - ...)
+    for (int k = fixtab::kSinTerms - 2; k >= 0; --k) b = kS[k] - mulhi(y, b);  // ~1/3! - y(1/5! - ...)
     const uint64_t sb = mulhi(y, b);                          // y * b
     const u128 Ws = sb ? (u128)Tm * ((uint64_t)0 - sb) : ((u128)Tm << 64);
     sv = round_u128_high(Ws, 122 + lz);  // Ws in [2^124, 2^127)
-    uint64_t c = kCo[9];
+    uint64_t c = kCo[fixtab::kCosTerms - 1];
 #pragma unroll
-    for (int k = 8; k >= 0; --k) c = kCo[k] - mulhi(y, c);  // 1/2! - y(1/4! - ...)
+    for (int k = fixtab::kCosTerms - 2; k >= 0; --k) c = kCo[k] - mulhi(y, c);  // ~1/2! - y(1/4! - ...)
     const uint64_t cb = mulhi(y, c);
     cv = cb ? round_unit_q64((uint64_t)0 - cb) : 1.0;  // cos >= cos(pi/4): 2^64 - cb >= 2^63
   }
