@@ -391,41 +391,45 @@ __device__ __forceinline__ void scatter_update(const MeshDev &m, const CellsDev 
 }
 
 // boundary condition of the crossed face: interior faces are ELEMENT
-// (proto_mesh.h:156-202)
+// (proto_mesh.h:156-202).  Selects rather than a switch: the few lanes of a
+// warp that cross a face in one loop trip cross different faces, and the
+// cases of a switch would run one after another.
 __device__ __forceinline__ int face_bc(const MeshDev &m, const Lane &L, uint32_t surface_cross) {
-  bool interior;
-  switch (surface_cross) {
-    case 0: interior = L.ci > 0; break;
-    case 1: interior = L.ci + 1 < m.ngx; break;
-    case 2: interior = L.cj > 0; break;
-    case 3: interior = L.cj + 1 < m.ngy; break;
-    case 4: interior = L.ck > 0; break;
-    default: interior = L.ck + 1 < m.ngz; break;
-  }
-  if (interior) return ELEMENT;
+  const uint32_t axis = surface_cross >> 1;
+  const bool up = (surface_cross & 1u) != 0u;
+  const uint32_t idx = axis == 0 ? L.ci : (axis == 1 ? L.cj : L.ck);
+  const uint32_t n = axis == 0 ? m.ngx : (axis == 1 ? m.ngy : m.ngz);
+  if (up ? idx + 1 < n : idx > 0) return ELEMENT;
   // constant indices: a variable index into the kernel parameter's array
   // would make the compiler copy the whole MeshDev to local memory
-  switch (surface_cross) {
-    case 0: return m.bc[0];
-    case 1: return m.bc[1];
-    case 2: return m.bc[2];
-    case 3: return m.bc[3];
-    case 4: return m.bc[4];
-    default: return m.bc[5];
-  }
+  int bc = m.bc[5];
+  bc = surface_cross == 4 ? m.bc[4] : bc;
+  bc = surface_cross == 3 ? m.bc[3] : bc;
+  bc = surface_cross == 2 ? m.bc[2] : bc;
+  bc = surface_cross == 1 ? m.bc[1] : bc;
+  bc = surface_cross == 0 ? m.bc[0] : bc;
+  return bc;
 }
 
 // ELEMENT crossing: the photon enters the neighbour (cell.h:110-112); only
-// the crossed axis gets a new face ahead
+// the crossed axis gets a new face ahead.  Selects, as in face_bc.
 template <bool kFaces = false>
 __device__ __forceinline__ void enter_neighbour(const MeshDev &m, Lane &L, uint32_t surface_cross) {
-  switch (surface_cross) {
-    case 0: --L.ci; L.cell -= 1; if constexpr (kFaces) L.fx = m.x[L.ci]; break;
-    case 1: ++L.ci; L.cell += 1; if constexpr (kFaces) L.fx = m.x[L.ci + 1]; break;
-    case 2: --L.cj; L.cell -= m.ngx; if constexpr (kFaces) L.fy = m.y[L.cj]; break;
-    case 3: ++L.cj; L.cell += m.ngx; if constexpr (kFaces) L.fy = m.y[L.cj + 1]; break;
-    case 4: --L.ck; L.cell -= m.ngx * m.ngy; if constexpr (kFaces) L.fz = m.z[L.ck]; break;
-    default: ++L.ck; L.cell += m.ngx * m.ngy; if constexpr (kFaces) L.fz = m.z[L.ck + 1]; break;
+  const uint32_t axis = surface_cross >> 1;
+  const bool up = (surface_cross & 1u) != 0u;
+  const uint32_t step = up ? 1u : 0xFFFFFFFFu;  // +1 or -1
+  const uint32_t stride = axis == 0 ? 1u : (axis == 1 ? m.ngx : m.ngx * m.ngy);
+  L.cell = up ? L.cell + stride : L.cell - stride;
+  L.ci += axis == 0 ? step : 0u;
+  L.cj += axis == 1 ? step : 0u;
+  L.ck += axis == 2 ? step : 0u;
+  if constexpr (kFaces) {
+    const double *planes = axis == 0 ? m.x : (axis == 1 ? m.y : m.z);
+    const uint32_t idx = (axis == 0 ? L.ci : (axis == 1 ? L.cj : L.ck)) + (up ? 1u : 0u);
+    const double f = planes[idx];
+    L.fx = axis == 0 ? f : L.fx;
+    L.fy = axis == 1 ? f : L.fy;
+    L.fz = axis == 2 ? f : L.fz;
   }
 }
 
