@@ -435,17 +435,22 @@ __device__ __forceinline__ void enter_neighbour(const MeshDev &m, Lane &L, uint3
 
 // REFLECT: Photon::reflect (photon.h:151-155): the direction cosine flips
 // and the face ahead on that axis becomes the opposite plane of the cell.
+// Selects, as in face_bc.
 template <bool kFaces = false>
 __device__ __forceinline__ void reflect(const MeshDev &m, Lane &L, uint32_t surface_cross) {
-  if (surface_cross < 2) {
-    L.dx = -L.dx;
-    if constexpr (kFaces) L.fx = m.x[L.ci + ((__double_as_longlong(L.dx) > 0) ? 1u : 0u)];
-  } else if (surface_cross < 4) {
-    L.dy = -L.dy;
-    if constexpr (kFaces) L.fy = m.y[L.cj + ((__double_as_longlong(L.dy) > 0) ? 1u : 0u)];
-  } else {
-    L.dz = -L.dz;
-    if constexpr (kFaces) L.fz = m.z[L.ck + ((__double_as_longlong(L.dz) > 0) ? 1u : 0u)];
+  const uint32_t axis = surface_cross >> 1;
+  constexpr long long kSign = (long long)0x8000000000000000ULL;  // negation as a sign-bit flip
+  L.dx = __longlong_as_double(__double_as_longlong(L.dx) ^ (axis == 0 ? kSign : 0LL));
+  L.dy = __longlong_as_double(__double_as_longlong(L.dy) ^ (axis == 1 ? kSign : 0LL));
+  L.dz = __longlong_as_double(__double_as_longlong(L.dz) ^ (axis == 2 ? kSign : 0LL));
+  if constexpr (kFaces) {
+    const double dir = axis == 0 ? L.dx : (axis == 1 ? L.dy : L.dz);
+    const double *planes = axis == 0 ? m.x : (axis == 1 ? m.y : m.z);
+    const uint32_t idx = (axis == 0 ? L.ci : (axis == 1 ? L.cj : L.ck)) + ((__double_as_longlong(dir) > 0) ? 1u : 0u);
+    const double f = planes[idx];
+    L.fx = axis == 0 ? f : L.fx;
+    L.fy = axis == 1 ? f : L.fy;
+    L.fz = axis == 2 ? f : L.fz;
   }
 }
 

@@ -119,29 +119,24 @@ __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
       } else {
         int bc = ELEMENT;
         if (ev == SEG_BOUNDARY) bc = face_bc(m, L, surface_cross);
-        if (ev != SEG_BOUNDARY || bc != REFLECT) {  // the visit to this cell ends
+        const bool moves_on = ev == SEG_BOUNDARY && bc == ELEMENT;
+        const bool turns = ev == SEG_BOUNDARY && bc == REFLECT;
+        if (!turns) {  // the visit to this cell ends
           flush = true;
           fcell = L.cell;
           fa = L.thr_abs;
           ft = visit_deposit(L, ev);
         }
-        if (ev == SEG_KILLED) {
-          store_end(b, L, KILLED);
-          active = false;
-          add_segments(seg_total, L.segs, d);
-        } else if (ev == SEG_CENSUS) {
-          store_end(b, L, CENSUS);
-          active = false;
-          add_segments(seg_total, L.segs, d);
-        } else if (bc == ELEMENT) {
+        if (moves_on) {
           L.thr_abs = 0.0;
           enter_neighbour(m, L, surface_cross);
-        } else if (bc == VACUUM || bc == SOURCE || bc == PROCESSOR) {
-          store_end(b, L, bc == PROCESSOR ? PASS : EXIT);
+        } else if (turns) {
+          reflect(m, L, surface_cross);
+        } else {  // the history ends: cutoff kill, census, or out through a domain face
+          const uint8_t desc = ev == SEG_KILLED ? KILLED : (ev == SEG_CENSUS ? CENSUS : (bc == PROCESSOR ? PASS : EXIT));
+          store_end(b, L, desc);
           active = false;
           add_segments(seg_total, L.segs, d);
-        } else {
-          reflect(m, L, surface_cross);
         }
       }
     }
