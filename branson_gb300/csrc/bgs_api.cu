@@ -378,6 +378,8 @@ int bgs_set_mesh(bgs_context *ctx, const bgs_mesh_desc *md) {
   m.x = x; m.y = y; m.z = z; m.region = region; m.regions = regions;
   for (int f = 0; f < 6; ++f) m.bc[f] = md->bc[f];
   m.T_source = md->T_source;
+  m.inv_ngx = div_multiplier(m.ngx);
+  m.inv_ngxy = div_multiplier((uint64_t)m.ngx * m.ngy);
   launch_init_cells(m, c, ctx->stream);
   BGS_LAUNCHED(ctx, 1);
   BGS_CUDA(ctx, cudaMemsetAsync(ctx->d_diag, 0, sizeof(DeviceDiag), ctx->stream));

@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(kEventThreads) k_event_boundary(MeshDev m, Cel
       p = es.q_boundary[w];
       Lane L;
       L.cell = b.cell[p];
-      L.ci = L.cell % m.ngx; L.cj = (L.cell / m.ngx) % m.ngy; L.ck = L.cell / (m.ngx * m.ngy);
+      cell_coords(m, L.cell, L.ci, L.cj, L.ck);
       const uint32_t sc = es.surface[p];
       const int bc = face_bc(m, L, sc);
       if (bc == ELEMENT || bc == VACUUM || bc == SOURCE || bc == PROCESSOR) {  // the visit ends

@@ -81,12 +81,35 @@ struct Bank {
 struct MeshDev {
   uint32_t ngx, ngy, ngz, n_groups;
   uint32_t n_cells, n_regions;
+  // floor(2^64 / d) + 1 for d = ngx and ngx*ngy (0 for d = 1): a cell's
+  // coordinates by multiplies instead of divisions (cell_coords)
+  unsigned long long inv_ngx, inv_ngxy;
   const double *x, *y, *z;
   const uint32_t *region;
   const double *regions;  // n_regions x 8
   int bc[6];
   double T_source;
 };
+
+// the multiplier of MeshDev::inv_ngx / inv_ngxy for divisor d >= 1
+inline unsigned long long div_multiplier(uint64_t d) {
+  return d <= 1 ? 0ULL : (unsigned long long)(((unsigned __int128)1 << 64) / d) + 1ULL;
+}
+
+// n / d for n, d < 2^32 from M = floor(2^64/d) + 1: n M / 2^64 exceeds n/d
+// by less than n / 2^64 < 2^-32 <= 1/d, which never carries past the next
+// integer (the fraction of n/d is at most 1 - 1/d)
+__device__ __forceinline__ uint32_t div_by_multiplier(uint32_t n, uint32_t d, unsigned long long M) {
+  return d <= 1 ? n : (uint32_t)__umul64hi((unsigned long long)n, M);
+}
+
+// (i, j, k) of cell g = i + ngx (j + ngy k)
+__device__ __forceinline__ void cell_coords(const MeshDev &m, uint32_t g, uint32_t &i, uint32_t &j, uint32_t &k) {
+  const uint32_t q = div_by_multiplier(g, m.ngx, m.inv_ngx);  // j + ngy k
+  k = div_by_multiplier(g, m.ngx * m.ngy, m.inv_ngxy);
+  i = g - q * m.ngx;
+  j = q - k * m.ngy;
+}
 
 struct CellsDev {
   double *T_e, *T_r, *T_s, *op_a, *op_s, *f, *em_E, *ce_E, *so_E, *T_r_diag;

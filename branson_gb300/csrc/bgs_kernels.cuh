@@ -8,7 +8,8 @@ namespace bgs {
 
 // node array of cell g (cell.h:325): (x_lo, x_hi, y_lo, y_hi, z_lo, z_hi)
 __device__ __forceinline__ void cell_nodes(const MeshDev &m, uint32_t g, double n[6]) {
-  const uint32_t i = g % m.ngx, j = (g / m.ngx) % m.ngy, k = g / (m.ngx * m.ngy);
+  uint32_t i, j, k;
+  cell_coords(m, g, i, j, k);
   n[0] = m.x[i];
   n[1] = m.x[i + 1];
   n[2] = m.y[j];

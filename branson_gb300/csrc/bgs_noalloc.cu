@@ -108,6 +108,8 @@ extern "C" BGS_API int bgs_transport_device_noalloc(
   m.region = nullptr; m.regions = nullptr;
   for (int k = 0; k < 6; ++k) m.bc[k] = bc[k];
   m.T_source = 0.0;
+  m.inv_ngx = div_multiplier(m.ngx);
+  m.inv_ngxy = div_multiplier((uint64_t)m.ngx * m.ngy);
   CellsDev c{};
   c.op_a = const_cast<double *>(op_a);
   c.op_s = const_cast<double *>(op_s);

@@ -457,9 +457,7 @@ __device__ __forceinline__ void reflect(const MeshDev &m, Lane &L, uint32_t surf
 // cell coordinates and the faces ahead from the global cell index
 template <bool kFaces = false>
 __device__ __forceinline__ void locate(const MeshDev &m, Lane &L) {
-  L.ci = L.cell % m.ngx;
-  L.cj = (L.cell / m.ngx) % m.ngy;
-  L.ck = L.cell / (m.ngx * m.ngy);
+  cell_coords(m, L.cell, L.ci, L.cj, L.ck);
   load_faces<kFaces>(m, L);
 }
 
