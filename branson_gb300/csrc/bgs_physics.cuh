@@ -62,8 +62,10 @@ __device__ __forceinline__ void load_faces(const MeshDev &m, Lane &L) {
 // a history's birth weight: the cutoff threshold RN(0.01 E0)
 __device__ __forceinline__ void set_birth(Lane &L, double E0) { L.kill_thr = kCutoff * E0; }
 
-// Warp-aggregated tally flush: every lane of the warp calls it (flush false
-// for lanes with nothing to add); lanes flushing into the same cell
+// Warp-aggregated tally flush of cell visits (a: the visit's absorbed
+// energy, t: the part of it a cutoff kill deposited; TallyCell): every lane
+// of the warp calls it (flush false for lanes with nothing to add); lanes
+// flushing into the same cell
 // (__match_any_sync on the cell, or on problem<<32|cell for the batched
 // kernel) add their 128-bit fixed-point contributions by shuffles and one
 // lane per cell issues the atomics.  Fixed-point sums are exact, so the
