@@ -339,12 +339,12 @@ BGS_HD SinCos sincos_phi_v(double phi) {
   }
   const double so = swap ? cv : sv;  // sin, cos of (t*pi/2)
   const double co = swap ? sv : cv;
-  switch (quad) {
-    case 0: return {so, co};
-    case 1: return {co, -so};
-    case 2: return {-so, -co};
-    default: return {-co, so};
-  }
+  // quadrant q: sin = (so, co, -so, -co)[q], cos = (co, -so, -co, so)[q], by
+  // selects and sign-bit flips (lanes of a warp hold different quadrants)
+  const uint64_t sgn = 0x8000000000000000ULL;
+  const uint64_t sb = double_to_bits((quad & 1u) ? co : so) ^ ((quad & 2u) ? sgn : 0ULL);
+  const uint64_t cb = double_to_bits((quad & 1u) ? so : co) ^ (((quad + 1u) & 2u) ? sgn : 0ULL);
+  return {bits_to_double(sb), bits_to_double(cb)};
 }
 
 BGS_HD void sincos_phi(double phi, double *s_out, double *c_out) {
