@@ -226,9 +226,12 @@ BGS_HD double exp_neg(double tau) {
   u128 T;
   if (sh >= 0) T = (u128)tm << sh;
   else T = sh > -64 ? (u128)(tm >> (-sh)) : (u128)0;
-  // N ~ floor(tau * 1024/ln2) from the top bits, then corrected exactly
-  const uint64_t A = (uint64_t)(T >> 44);  // tau * 2^52
-  uint64_t N = mulhi(A, fixtab::kInvLn2_1024_q12);
+  // N ~ floor(tau * 1024/ln2) from the top bits, then corrected exactly.
+  // The estimate (tau to 2^-32, a 43-bit multiplier) is off by less than
+  // 4e-7 before the floor, so the corrections almost never run (a warp's
+  // lanes seldom diverge there)
+  const uint64_t A = (uint64_t)(T >> 64);  // tau * 2^32
+  uint64_t N = mulhi(A, fixtab::kInvLn2_1024_q32);
   const u128 L = ((u128)fixtab::kLn2_1024_96_hi << 64) | fixtab::kLn2_1024_96_lo;
   u128 NL = L * N;
 #pragma unroll 1

@@ -7,7 +7,7 @@ and rounded to nearest:
   EXP2_NEG[j] = 2^(63 - j/1024)       j = 0..1023
   LN2_120     = ln 2 * 2^120          (hi, lo)
   LN2_1024_96 = ln 2 / 1024 * 2^96    (hi, lo)
-  K_1024_LN2  = 1024/ln 2 * 2^12      (estimate multiplier for the exp reduction)
+  K_1024_LN2  = 1024/ln 2 * 2^32      (estimate multiplier for the exp reduction)
   2/pi * 2^128, pi/2 * 2^62, and in Q64 the magnitudes of the coefficients
   of the sin/cos polynomials (below)
 
@@ -91,14 +91,14 @@ def main():
     exp2 = [rnd(Decimal(2) ** (Decimal(63) - Decimal(j) / N)) for j in range(N)]
     ln2_120 = rnd(LN2 * Decimal(2) ** 120)
     ln2_1024_96 = rnd(LN2 / N * Decimal(2) ** 96)
-    k = rnd(Decimal(N) / LN2 * Decimal(2) ** 12)
+    k = rnd(Decimal(N) / LN2 * Decimal(2) ** 32)
     assert all(0 < v < 2 ** 64 for v in invf[1:]) and all(0 < v <= 2 ** 63 for v in exp2)
     out = ["// Generated by gen_fixmath_tables.py (decimal, 80 digits); do not edit.",
            "#pragma once", "#include <cstdint>", "", "namespace bgs {", "namespace fixtab {",
            f"constexpr int kBins = {N};",
            "constexpr uint64_t kLn2_120_hi = 0x%016xULL, kLn2_120_lo = 0x%016xULL;" % hi_lo(ln2_120),
            "constexpr uint64_t kLn2_1024_96_hi = 0x%016xULL, kLn2_1024_96_lo = 0x%016xULL;" % hi_lo(ln2_1024_96),
-           "constexpr uint64_t kInvLn2_1024_q12 = 0x%016xULL;" % k, ""]
+           "constexpr uint64_t kInvLn2_1024_q32 = 0x%016xULL;" % k, ""]
 
     def table(name, vals, per=4):
         lines = [f"#define BGS_{name}_INIT \\"]
