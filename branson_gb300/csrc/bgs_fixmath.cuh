@@ -112,25 +112,19 @@ BGS_HD uint64_t double_to_bits(double d) {
 #endif
 }
 
-// Round the positive value W * 2^-scale (W != 0) to the nearest double.
-// Values below the normal range flush to zero (callers never produce them
-// on the paths that use this).
-BGS_HD double round_u128(u128 W, int scale) {
+// The positive value W * 2^-scale rounded to the nearest double, for a W
+// whose top set bit is at 117 or above, so the mantissa and the rounding
+// position both lie in the high word (the sine and exp results): one 64-bit
+// shift and compare.  Values below the normal range flush to zero (callers
+// never produce them on the paths that use this).
+BGS_HD double round_u128_high(u128 W, int scale) {
   const uint64_t hi = (uint64_t)(W >> 64), lo = (uint64_t)W;
-  const int p = hi ? 127 - clz64(hi) : 63 - clz64(lo);  // top set bit
-  uint64_t mant;
-  bool up;
-  if (p >= 53) {
-    const int sh = p - 52;  // bits dropped
-    mant = (uint64_t)(W >> sh);
-    const u128 rem = W & (((u128)1 << sh) - 1);
-    const u128 half = (u128)1 << (sh - 1);
-    up = rem > half || (rem == half && (mant & 1));
-  } else {
-    mant = (uint64_t)(W << (52 - p));
-    up = false;
-  }
-  int e2 = p - scale;  // value = mant * 2^(e2 - 52)
+  const int ph = 63 - clz64(hi);  // top set bit of W is ph + 64
+  const int sh = ph - 52;         // bits of hi below the mantissa, >= 1
+  uint64_t mant = hi >> sh;
+  const uint64_t rem = hi & ((1ULL << sh) - 1), half = 1ULL << (sh - 1);
+  const bool up = rem > half || (rem == half && (lo != 0 || (mant & 1)));
+  int e2 = ph + 64 - scale;  // value = mant * 2^(e2 - 52)
   if (up) {
     ++mant;
     if (mant >> 53) { mant >>= 1; ++e2; }
@@ -140,17 +134,20 @@ BGS_HD double round_u128(u128 W, int scale) {
   return bits_to_double(((uint64_t)be << 52) | (mant & 0x000FFFFFFFFFFFFFULL));
 }
 
-// round_u128 for a W whose top set bit is at 117 or above, so the mantissa
-// and the rounding position both lie in the high word (the sine and exp
-// results): one 64-bit shift and compare instead of 128-bit ones.
-BGS_HD double round_u128_high(u128 W, int scale) {
+// The same for any W with a nonzero high word (the log results): W is first
+// normalised so its top bit is bit 127 (a funnel shift by clz, branch-free),
+// then the mantissa and rounding bit sit at fixed positions of the high
+// word, as in round_u128_high.  The log's results span both sides of the
+// word boundary of the generic shift, which made lanes of a warp diverge.
+BGS_HD double round_u128_norm(u128 W, int scale) {
   const uint64_t hi = (uint64_t)(W >> 64), lo = (uint64_t)W;
-  const int ph = 63 - clz64(hi);  // top set bit of W is ph + 64
-  const int sh = ph - 52;         // bits of hi below the mantissa, >= 1
-  uint64_t mant = hi >> sh;
-  const uint64_t rem = hi & ((1ULL << sh) - 1), half = 1ULL << (sh - 1);
-  const bool up = rem > half || (rem == half && (lo != 0 || (mant & 1)));
-  int e2 = ph + 64 - scale;  // value = mant * 2^(e2 - 52)
+  const int lz = clz64(hi);                                   // < 64: hi != 0
+  const uint64_t nh = (hi << lz) | (lz ? lo >> (64 - lz) : 0ULL);
+  const uint64_t nl = lo << lz;
+  uint64_t mant = nh >> 11;
+  const uint64_t rem = nh & 0x7FFULL;
+  const bool up = rem > 0x400ULL || (rem == 0x400ULL && (nl != 0 || (mant & 1)));
+  int e2 = 127 - lz - scale;  // value = mant * 2^(e2 - 52)
   if (up) {
     ++mant;
     if (mant >> 53) { mant >>= 1; ++e2; }
@@ -185,7 +182,7 @@ BGS_HD double neg_log_u53(uint64_t m) {
     t = 0x8000000000000000ULL + mulhi(V, t);       // 1/2
     const uint64_t T = mulhi(V, t);                // (S - 1) * 2^64
     const u128 L = ((u128)V << 64) + (u128)V * T;  // L * 2^128
-    return round_u128(L, 128);
+    return round_u128_norm(L, 128);
   }
   const int e = 63 - clz64(m);                     // m in [2^e, 2^(e+1))
   const uint64_t k = 53 - e;                       // u = x 2^-k, x in [1, 2)
@@ -208,7 +205,7 @@ BGS_HD double neg_log_u53(uint64_t m) {
   W -= log_lnf(j);
   W -= (u128)R << 46;
   W += (u128)Q << 36;
-  return round_u128(W, 120);
+  return round_u128_norm(W, 120);  // W >= 2^108: the result is above 2^-12
 }
 
 // exp(-tau) for tau >= 0: the factor exp(-sigma_a*f*d) of the implicit-capture
