@@ -43,6 +43,17 @@ def _offset_scatter_deck():
                 regions=[Region(1, 0.1, 1.0, 300.0, 0.0, 0.0, 500.0, 0.3, 0.3)])
 
 
+def _column_deck():
+    """One cell across x (so the cell coordinates divide by ngx = 1), 5 x 7
+    cells in y and z, reflecting x faces, a 0.5 keV source on z-."""
+    from branson_gb300.deck import Deck, Division, Region, REFLECT, SOURCE, VACUUM
+    return Deck(t_start=0.0, t_stop=0.02, dt_start=0.01, t_mult=1.0, dt_max=1.0, photons=20000, seed=9,
+                x_divisions=[Division(0.0, 0.3, 1)], y_divisions=[Division(0.0, 0.5, 5)],
+                z_divisions=[Division(0.0, 0.7, 7)], region_map={(0, 0, 0): 1},
+                bc=(REFLECT, REFLECT, VACUUM, VACUUM, SOURCE, VACUUM), T_source=0.5,
+                regions=[Region(1, 0.1, 1.0, 20.0, 0.0, 0.0, 2.0, 0.1, 0.1)])
+
+
 def _decks():
     from branson_gb300 import deck as D
     return {
@@ -51,6 +62,7 @@ def _decks():
         "hohlraum30": D.hohlraum(n_per_axis=10, photons=20000, n_steps=2, n_groups=30),
         "uniform8": _uniform_deck(),
         "offset_scatter": _offset_scatter_deck(),
+        "column": _column_deck(),
     }
 
 
@@ -59,7 +71,7 @@ def _extent(dk):
     return max(x[-1] - x[0], y[-1] - y[0], z[-1] - z[0], C_LIGHT * dk.dt_start)
 
 
-@pytest.mark.parametrize("name", ["marshak", "hot_zone", "hohlraum30", "offset_scatter"])
+@pytest.mark.parametrize("name", ["marshak", "hot_zone", "hohlraum30", "offset_scatter", "column"])
 def test_dropin_transport_matches_oracle(gpu_lib, name):
     import oracle as O
     from branson_gb300.engine import ReplicatedIMC, arrays_to_records, records_to_arrays
@@ -100,7 +112,7 @@ def test_dropin_transport_matches_oracle(gpu_lib, name):
         gpu.close()
 
 
-@pytest.mark.parametrize("name", ["marshak", "hot_zone", "hohlraum30", "uniform8", "offset_scatter"])
+@pytest.mark.parametrize("name", ["marshak", "hot_zone", "hohlraum30", "uniform8", "offset_scatter", "column"])
 def test_device_step_matches_oracle(gpu_lib, name):
     import oracle as O
     from branson_gb300.engine import ReplicatedIMC, arrays_to_records
