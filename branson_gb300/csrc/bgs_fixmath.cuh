@@ -125,10 +125,10 @@ BGS_HD double round_u128_high(u128 W, int scale) {
   const uint64_t rem = hi & ((1ULL << sh) - 1), half = 1ULL << (sh - 1);
   const bool up = rem > half || (rem == half && (lo != 0 || (mant & 1)));
   int e2 = ph + 64 - scale;  // value = mant * 2^(e2 - 52)
-  if (up) {
-    ++mant;
-    if (mant >> 53) { mant >>= 1; ++e2; }
-  }
+  mant += up ? 1ULL : 0ULL;  // data-dependent: no branch, so no split warp
+  const int carry = (int)(mant >> 53);
+  mant >>= carry;
+  e2 += carry;
   const int be = e2 + 1023;
   if (be <= 0) return 0.0;
   return bits_to_double(((uint64_t)be << 52) | (mant & 0x000FFFFFFFFFFFFFULL));
@@ -148,10 +148,10 @@ BGS_HD double round_u128_norm(u128 W, int scale) {
   const uint64_t rem = nh & 0x7FFULL;
   const bool up = rem > 0x400ULL || (rem == 0x400ULL && (nl != 0 || (mant & 1)));
   int e2 = 127 - lz - scale;  // value = mant * 2^(e2 - 52)
-  if (up) {
-    ++mant;
-    if (mant >> 53) { mant >>= 1; ++e2; }
-  }
+  mant += up ? 1ULL : 0ULL;  // data-dependent: no branch, so no split warp
+  const int carry = (int)(mant >> 53);
+  mant >>= carry;
+  e2 += carry;
   const int be = e2 + 1023;
   if (be <= 0) return 0.0;
   return bits_to_double(((uint64_t)be << 52) | (mant & 0x000FFFFFFFFFFFFFULL));
@@ -399,7 +399,9 @@ BGS_HD double sqrt_rn(double x) {
   }
   uint64_t M = (xb & 0x000FFFFFFFFFFFFFULL) | 0x0010000000000000ULL;
   int e = ex - 1075;  // x = M * 2^e
-  if (e & 1) { M <<= 1; --e; }  // e even, 2^52 <= M < 2^54
+  const int odd = e & 1;  // e even, 2^52 <= M < 2^54 (a shift, not a branch)
+  M <<= odd;
+  e -= odd;
   const u128 N = (u128)M << 52;  // sqrt(x) = sqrt(N) * 2^((e-52)/2), sqrt(N) in [2^52, 2^53)
   const uint64_t W = M << 10;    // w = M/2^54 in [1/4, 1), Q64
   const float wf = u64_to_float_approx(M >> 30) * (1.0f / 16777216.0f);
@@ -431,7 +433,7 @@ BGS_HD double sqrt_rn(double x) {
     ++y;
   }
   // nearest: N - y^2 > y  <=>  sqrt(N) > y + 1/2 (no exact ties)
-  if (N - sq > (u128)y) ++y;
+  y += (N - sq > (u128)y) ? 1ULL : 0ULL;
   int eo = (e - 52) / 2 + 52;  // value = y * 2^(eo - 52)
   if (y >> 53) { y >>= 1; ++eo; }
   return bits_to_double(((uint64_t)(eo + 1023) << 52) | (y & 0x000FFFFFFFFFFFFFULL));
