@@ -254,10 +254,16 @@ __device__ __forceinline__ bool approx_faces(double ax, double ay, double az, co
   const float kInf = __int_as_float(0x7f800000);
   ok &= !(qx >= kLo && qx <= kHi) & !(qy >= kLo && qy <= kHi) & !(qz >= kLo && qz <= kHi);
   const float cx = qx < kLo ? qx : kInf, cy = qy < kLo ? qy : kInf, cz = qz < kLo ? qz : kInf;
-  int j = 0;
-  float m = cx, second = fminf(cy, cz);
-  if (cy < m) { j = 1; m = cy; second = fminf(cx, cz); }
-  if (cz < m) { j = 2; m = cz; second = fminf(cx, cy); }
+  // the first smallest (x, then y, then z) and the smallest of the others,
+  // by selects: which face wins differs from lane to lane
+  const bool y_first = cy < cx;
+  int j = y_first ? 1 : 0;
+  float m = y_first ? cy : cx;
+  float second = y_first ? fminf(cx, cz) : fminf(cy, cz);
+  const bool z_first = cz < m;
+  j = z_first ? 2 : j;
+  second = z_first ? fminf(cx, cy) : second;
+  m = z_first ? cz : m;
   if (m != kInf) ok &= (second == kInf) || (second - m > kTol * (fabsf(second) + fabsf(m)));
   if (!ok) return false;
   if (m == kInf) {  // no face closer than 1e16
