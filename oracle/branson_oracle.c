@@ -22,6 +22,35 @@ static const double BO_C = 299.792458;  /* cm/shake */
 static const double BO_A = 0.01372;     /* GJ/cm^3/keV^4 */
 static const double BO_CUTOFF = 0.01;
 
+/* The transcendental functions of the photon arithmetic.  The default build
+ * calls the host libm, as the upstream code does: that build is the oracle.
+ * The BO_GPU_MATH build (make -C oracle gpumath) is a diagnostic twin: the
+ * same C with -log(u), exp(x) and sin/cos(phi) taken from the GPU path's
+ * integer fixed-point routines compiled for the host (oracle/gpu_math.cc),
+ * and the boundary-source polar angle from cos(acos(sqrt u)) = sqrt(u),
+ * sin(acos(sqrt u)) = sqrt(1 - u), as the GPU sources it.  Everything else
+ * is IEEE arithmetic in the upstream order in both builds, so a history on
+ * which the GPU and the oracle disagree, while the GPU and the twin agree,
+ * differs only through the last-bit rounding of those functions; the
+ * per-segment trace (bo_trace_photon) of both builds then locates the
+ * comparison at which the two paths parted. */
+#ifdef BO_GPU_MATH
+double bo_gm_neg_log_u53(uint64_t m);
+double bo_gm_exp_neg(double t);
+void bo_gm_sincos_phi(double phi, double *s, double *c);
+/* u is an RNG draw m * 2^-53 (odd m < 2^53), so m is recovered exactly */
+static inline double neg_log_u(double u) { return bo_gm_neg_log_u53((uint64_t)(u * 9007199254740992.0)); }
+static inline double exp_of(double x) { return bo_gm_exp_neg(-x); }
+static inline void sincos_of(double phi, double *s, double *c) { bo_gm_sincos_phi(phi, s, c); }
+#else
+static inline double neg_log_u(double u) { return -log(u); }
+static inline double exp_of(double x) { return exp(x); }
+static inline void sincos_of(double phi, double *s, double *c) {
+  *s = sin(phi);
+  *c = cos(phi);
+}
+#endif
+
 /* ------------------------------------------------------------------------ */
 /* Threefry2x64 with 20 rounds, restated from the published Random123
  * specification (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as
@@ -286,29 +315,39 @@ static void uniform_angle(bo_rng *r, double dir[3]) {
   const double mu = rng_next(r) * 2.0 - 1.0;
   const double phi = rng_next(r) * 2.0 * BO_PI;
   const double sin_theta = sqrt(1.0 - mu * mu);
-  dir[0] = sin_theta * cos(phi);
-  dir[1] = sin_theta * sin(phi);
+  double sp, cp;
+  sincos_of(phi, &sp, &cp);
+  dir[0] = sin_theta * cp;
+  dir[1] = sin_theta * sp;
   dir[2] = mu;
 }
 
 /* get_source_angle_on_face (sampling_functions.h:94-121); only the x faces
  * carry the inward sign, as upstream. */
 static void source_angle_on_face(bo_rng *r, int face, double dir[3]) {
+#ifdef BO_GPU_MATH
+  const double u = rng_next(r);
+  const double ct = sqrt(u), st = sqrt(1.0 - u);
+#else
   const double theta = acos(sqrt(rng_next(r)));
+  const double ct = cos(theta), st = sin(theta);
+#endif
   const double phi = rng_next(r) * 2.0 * BO_PI;
   const double sign = (face % 2) ? -1.0 : 1.0;
+  double sp, cp;
+  sincos_of(phi, &sp, &cp);
   if (face == 0 || face == 1) {
-    dir[0] = cos(theta) * sign;
-    dir[1] = sin(theta) * sin(phi);
-    dir[2] = sin(theta) * cos(phi);
+    dir[0] = ct * sign;
+    dir[1] = st * sp;
+    dir[2] = st * cp;
   } else if (face == 2 || face == 3) {
-    dir[0] = sin(theta) * sin(phi);
-    dir[1] = cos(theta);
-    dir[2] = sin(theta) * cos(phi);
+    dir[0] = st * sp;
+    dir[1] = ct;
+    dir[2] = st * cp;
   } else {
-    dir[0] = sin(theta) * cos(phi);
-    dir[1] = sin(theta) * sin(phi);
-    dir[2] = cos(theta);
+    dir[0] = st * cp;
+    dir[1] = st * sp;
+    dir[2] = ct;
   }
 }
 
@@ -375,42 +414,69 @@ static void initial_census_photon(const bo_mesh *m, uint32_t g, double E, double
   p->descriptor = BO_PASS;
 }
 
-/* make_photons (source.h:294-366), rank 0: stream = 1e13*cycle + ith. */
+/* make_photons (source.h:294-366), rank 0: stream = 1e13*cycle + ith.  The
+ * upstream loop walks the cells in order with a running photon index ith;
+ * every photon depends only on its cell, its energy and its stream, so the
+ * cells are made in parallel from the prefix sums of their counts (the same
+ * photons at the same list positions, only faster to build). */
 void bo_make_photons(const bo_mesh *m, const bo_cells *c, double dt, uint32_t cycle, uint32_t seed,
                      uint64_t n_user, double total_E, bo_photon *out) {
   const uint32_t n = m->ngx * m->ngy * m->ngz;
   const uint64_t cycle_offset = 10000000000000ULL * (uint64_t)cycle;
+  uint64_t *first = (uint64_t *)malloc(((size_t)n + 1) * sizeof(uint64_t));
   uint64_t ith = 0;
   for (uint32_t g = 0; g < n; ++g) {
+    first[g] = ith;
+    ith += photons_for(n_user, c->emission_E[g], total_E) + photons_for(n_user, c->source_E[g], total_E);
+  }
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 64)
+#endif
+  for (long gl = 0; gl < (long)n; ++gl) {
+    const uint32_t g = (uint32_t)gl;
+    uint64_t k = first[g];
     const uint32_t n_em = photons_for(n_user, c->emission_E[g], total_E);
     if (n_em) {
       const double E = c->emission_E[g] / n_em;
-      for (uint32_t p = 0; p < n_em; ++p, ++ith)
-        emission_photon(m, g, E, dt, seed, cycle_offset + ith, &out[ith]);
+      for (uint32_t p = 0; p < n_em; ++p, ++k)
+        emission_photon(m, g, E, dt, seed, cycle_offset + k, &out[k]);
     }
     const uint32_t n_so = photons_for(n_user, c->source_E[g], total_E);
     if (n_so) {
       const double E = c->source_E[g] / n_so;
       const int face = cell_source_face(m, g);
-      for (uint32_t p = 0; p < n_so; ++p, ++ith)
-        boundary_source_photon(m, g, E, dt, seed, cycle_offset + ith, face, &out[ith]);
+      for (uint32_t p = 0; p < n_so; ++p, ++k)
+        boundary_source_photon(m, g, E, dt, seed, cycle_offset + k, face, &out[k]);
     }
   }
+  free(first);
 }
 
-/* make_initial_census_photons (source.h:183-204), rank 0: stream = ith. */
+/* make_initial_census_photons (source.h:183-204), rank 0: stream = ith;
+ * cells in parallel from the prefix sums of their counts, as above. */
 void bo_make_initial_census(const bo_mesh *m, const bo_cells *c, double dt, uint32_t seed,
                             uint64_t n_user, double total_E, bo_photon *out) {
   const uint32_t n = m->ngx * m->ngy * m->ngz;
+  uint64_t *first = (uint64_t *)malloc(((size_t)n + 1) * sizeof(uint64_t));
   uint64_t ith = 0;
   for (uint32_t g = 0; g < n; ++g) {
+    first[g] = ith;
+    ith += photons_for(n_user, c->census_E[g], total_E);
+  }
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 64)
+#endif
+  for (long gl = 0; gl < (long)n; ++gl) {
+    const uint32_t g = (uint32_t)gl;
+    uint64_t k = first[g];
     const uint32_t n_ce = photons_for(n_user, c->census_E[g], total_E);
     if (n_ce) {
       const double E = c->census_E[g] / n_ce;
-      for (uint32_t p = 0; p < n_ce; ++p, ++ith)
-        initial_census_photon(m, g, E, dt, seed, ith, &out[ith]);
+      for (uint32_t p = 0; p < n_ce; ++p, ++k)
+        initial_census_photon(m, g, E, dt, seed, k, &out[k]);
     }
   }
+  free(first);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -440,8 +506,9 @@ static uint32_t sample_emission_group(bo_rng *r, double op_a, uint32_t n_groups)
  * is tracked by its (i, j, k) position so that nodes, neighbours and
  * boundary codes come from the plane arrays without any division, the way
  * the upstream loop reads them from its precomputed Cell. */
-static uint64_t transport_photon(const bo_mesh *m, const bo_cells *c, uint32_t seed, bo_photon *p,
-                                 double *abs_t, double *track_t) {
+static inline __attribute__((always_inline)) uint64_t
+transport_photon_traced(const bo_mesh *m, const bo_cells *c, uint32_t seed, bo_photon *p, double *abs_t,
+                        double *track_t, bo_trace_rec *trace, size_t trace_cap) {
   bo_rng r;
   rng_init(&r, seed, p->stream, p->counter);
   uint32_t surface_cross = 0;
@@ -454,18 +521,24 @@ static uint64_t transport_photon(const bo_mesh *m, const bo_cells *c, uint32_t s
   int active = 1;
   while (active) {
     ++segments;
+    const uint32_t seg_cell = cell;
+    (void)seg_cell;
     const double sigma_s = c->op_s[cell];
     const double sigma_a = c->op_a[cell];
     const double f = c->f[cell];
     const double total_sigma_s = (1.0 - f) * sigma_a + sigma_s;
     const double dist_to_scatter =
-        (total_sigma_s > 0.0) ? -log(rng_next(&r)) / total_sigma_s : 1.0e100;
+        (total_sigma_s > 0.0) ? neg_log_u(rng_next(&r)) / total_sigma_s : 1.0e100;
     const double dist_to_boundary = distance_to_boundary(nodes, p->pos, p->dir, &surface_cross);
+    double face_q[3] = {0.0, 0.0, 0.0};
+    if (trace)
+      for (uint32_t i = 0; i < 3; ++i)
+        face_q[i] = (nodes[2 * i + (uint32_t)(0.0 < p->dir[i])] - p->pos[i]) / p->dir[i];
     const double dist_to_census = p->life_dx;
     /* std::min(a, b) is (b < a) ? b : a */
     const double db_dc = (dist_to_census < dist_to_boundary) ? dist_to_census : dist_to_boundary;
     const double dist_to_event = (db_dc < dist_to_scatter) ? db_dc : dist_to_scatter;
-    const double absorbed_E = p->E * (1.0 - exp(-sigma_a * f * dist_to_event));
+    const double absorbed_E = p->E * (1.0 - exp_of(-sigma_a * f * dist_to_event));
     thread_abs += absorbed_E;
     thread_track += absorbed_E / (sigma_a * f);
     p->E = p->E - absorbed_E;
@@ -530,9 +603,41 @@ static uint64_t transport_photon(const bo_mesh *m, const bo_cells *c, uint32_t s
       abs_t[cell] += thread_abs;
       track_t[cell] += thread_track;
     }
+    if (trace && segments <= trace_cap) {
+      bo_trace_rec *t = &trace[segments - 1];
+      t->d_scatter = dist_to_scatter;
+      t->d_boundary = dist_to_boundary;
+      t->d_census = dist_to_census;
+      t->face_q[0] = face_q[0];
+      t->face_q[1] = face_q[1];
+      t->face_q[2] = face_q[2];
+      t->E = p->E;
+      t->E0 = p->E0;
+      t->cell = seg_cell;
+      t->descriptor = p->descriptor;
+      t->surface = surface_cross;
+      t->counter = (uint32_t)r.counter;
+    }
   }
   p->counter = r.counter;
   return segments;
+}
+
+static uint64_t transport_photon(const bo_mesh *m, const bo_cells *c, uint32_t seed, bo_photon *p,
+                                 double *abs_t, double *track_t) {
+  return transport_photon_traced(m, c, seed, p, abs_t, track_t, NULL, 0);
+}
+
+size_t bo_trace_photon(const bo_mesh *m, const bo_cells *c, uint32_t seed, const bo_photon *start,
+                       bo_trace_rec *out, size_t max_segments, bo_photon *end) {
+  const size_t n_cells = (size_t)m->ngx * m->ngy * m->ngz;
+  double *t = (double *)calloc(2 * n_cells, sizeof(double));
+  bo_photon p = *start;
+  const uint64_t segs = transport_photon_traced(m, c, seed, &p, t, t + n_cells, out, max_segments);
+  free(t);
+  if (end)
+    *end = p;
+  return (size_t)segs;
 }
 
 /* history_cpu_transport_photons (history_based_transport.h:279-308):
@@ -766,12 +871,12 @@ static double adjoint_replay_photon(const bo_mesh *m, const bo_cells *c, const b
     const double f = c->f[cell];
     const double total_sigma_s = (1.0 - f) * sigma_a + sigma_s;
     const double dist_to_scatter =
-        (total_sigma_s > 0.0) ? -log(rng_next(&r)) / total_sigma_s : 1.0e100;
+        (total_sigma_s > 0.0) ? neg_log_u(rng_next(&r)) / total_sigma_s : 1.0e100;
     const double dist_to_boundary = distance_to_boundary(nodes, p->pos, p->dir, &surface_cross);
     const double dist_to_census = p->life_dx;
     const double db_dc = (dist_to_census < dist_to_boundary) ? dist_to_census : dist_to_boundary;
     const double dist_to_event = (db_dc < dist_to_scatter) ? db_dc : dist_to_scatter;
-    const double absorbed_E = p->E * (1.0 - exp(-sigma_a * f * dist_to_event));
+    const double absorbed_E = p->E * (1.0 - exp_of(-sigma_a * f * dist_to_event));
     p->E = p->E - absorbed_E;
     p->pos[0] += p->dir[0] * dist_to_event;
     p->pos[1] += p->dir[1] * dist_to_event;

@@ -96,6 +96,23 @@ void bo_make_initial_census(const bo_mesh *m, const bo_cells *c, double dt, uint
 uint64_t bo_transport(const bo_mesh *m, const bo_cells *c, uint32_t seed, bo_photon *photons,
                       size_t n, double *abs_E, double *track_E, int n_threads);
 
+/* One segment of a traced history: the three event distances the loop
+ * compares (history_based_transport.h:56-67), the three face quotients
+ * get_distance_to_boundary takes the smallest of (cell.h:117-132), the
+ * weight after the segment (for the cutoff test E/E0 < 0.01,
+ * photon.h:47-49), the cell the segment ran in, the descriptor it ended
+ * with, the face picked, and the low word of the RNG counter after it. */
+typedef struct {
+  double d_scatter, d_boundary, d_census, face_q[3], E, E0;
+  uint32_t cell, descriptor, surface, counter;
+} bo_trace_rec;
+
+/* transport_photon on one photon with a per-segment trace: up to
+ * max_segments records go to out; returns the number of segments; the end
+ * state goes to *end (may be NULL). */
+size_t bo_trace_photon(const bo_mesh *m, const bo_cells *c, uint32_t seed, const bo_photon *start,
+                       bo_trace_rec *out, size_t max_segments, bo_photon *end);
+
 /* post_process_photons (post_process_functions.h:33-59): census photons are
  * copied in order into census_out (may be NULL to count only).  Returns the
  * census size. */

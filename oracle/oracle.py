@@ -23,7 +23,11 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libbranson_oracle.so")
+# the diagnostic twin: the same C with the GPU path's integer -log/exp/sin/cos
+# in place of libm (branson_oracle.c, BO_GPU_MATH); math="gpu" selects it
+GPU_MATH_LIB_PATH = os.path.join(HERE, "_build", "libbranson_oracle_gpumath.so")
 REF_DIR = os.path.join(HERE, "_ref")
+FIXMATH_DIR = os.path.join(os.path.dirname(HERE), "branson_gb300", "csrc")
 
 # bo_photon / harness record (104 bytes)
 PHOTON_DTYPE = np.dtype([
@@ -36,10 +40,23 @@ C_LIGHT = 299.792458
 EXIT, PASS, CENSUS, SCATTER, KILLED, BOUND = range(6)
 
 
-def build(force: bool = False) -> str:
-    """Compile the C restatement with gcc (make -C oracle port)."""
-    if force or not os.path.exists(LIB_PATH) or \
-            os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, "branson_oracle.c")):
+def _stale(target: str, sources) -> bool:
+    return not os.path.exists(target) or any(os.path.getmtime(target) < os.path.getmtime(s) for s in sources)
+
+
+def build(force: bool = False, math: str = "libm") -> str:
+    """Compile the C restatement with gcc (make -C oracle port), or its
+    GPU-math twin (make -C oracle gpumath)."""
+    srcs = [os.path.join(HERE, "branson_oracle.c"), os.path.join(HERE, "branson_oracle.h")]
+    if math == "gpu":
+        srcs += [os.path.join(HERE, "gpu_math.cc"), os.path.join(FIXMATH_DIR, "bgs_fixmath.cuh"),
+                 os.path.join(FIXMATH_DIR, "bgs_fixmath_tables.h")]
+        if force or _stale(GPU_MATH_LIB_PATH, srcs):
+            subprocess.run(["make", "-s", "-C", HERE, "gpumath"], check=True)
+        return GPU_MATH_LIB_PATH
+    if math != "libm":
+        raise ValueError("math is 'libm' (the oracle) or 'gpu' (its GPU-math twin)")
+    if force or _stale(LIB_PATH, srcs):
         subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
     return LIB_PATH
 
@@ -64,14 +81,24 @@ class _Energy(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("total_photon_E", "emission_E", "census_E", "source_E", "pre_mat_E")]
 
 
-_lib = None
+class TraceRec(C.Structure):
+    _fields_ = [("d_scatter", C.c_double), ("d_boundary", C.c_double), ("d_census", C.c_double),
+                ("face_q", C.c_double * 3), ("E", C.c_double), ("E0", C.c_double), ("cell", C.c_uint32),
+                ("descriptor", C.c_uint32), ("surface", C.c_uint32), ("counter", C.c_uint32)]
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        build()
-        L = C.CDLL(LIB_PATH)
+TRACE_DTYPE = np.dtype([("d_scatter", "<f8"), ("d_boundary", "<f8"), ("d_census", "<f8"),
+                        ("face_q", "<f8", (3,)), ("E", "<f8"), ("E0", "<f8"), ("cell", "<u4"),
+                        ("descriptor", "<u4"), ("surface", "<u4"), ("counter", "<u4")])
+assert TRACE_DTYPE.itemsize == C.sizeof(TraceRec)
+
+_libs = {}
+
+
+def lib(math: str = "libm"):
+    if math not in _libs:
+        path = build(math=math)
+        L = C.CDLL(path)
         dp = C.POINTER(C.c_double)
         pp = C.c_void_p
         L.bo_rng_draw.restype = C.c_double
@@ -106,8 +133,10 @@ def lib():
         L.bo_adjoint_reweighted.restype = C.c_double
         L.bo_adjoint_reweighted.argtypes = [C.POINTER(_Mesh), C.POINTER(_Cells), dp, dp, C.c_uint32, pp,
                                             C.c_size_t, dp]
-        _lib = L
-    return _lib
+        L.bo_trace_photon.restype = C.c_size_t
+        L.bo_trace_photon.argtypes = [C.POINTER(_Mesh), C.POINTER(_Cells), C.c_uint32, pp, pp, C.c_size_t, pp]
+        _libs[math] = L
+    return _libs[math]
 
 
 def _dptr(a: np.ndarray):
@@ -163,9 +192,11 @@ class StepResult:
 class Oracle:
     """CPU replicated IMC problem driven through the C restatement."""
 
-    def __init__(self, deck, n_threads: int = 1):
+    def __init__(self, deck, n_threads: int = 1, math: str = "libm"):
         self.deck = deck
         self.n_threads = n_threads
+        self.math = math
+        self.L = lib(math)
         x, y, z = deck.planes()
         self._keep = [np.ascontiguousarray(x), np.ascontiguousarray(y), np.ascontiguousarray(z),
                       deck.cell_regions()]
@@ -179,7 +210,7 @@ class Oracle:
         self.arr = {k: np.zeros(self.n_cells) for k in
                     ("T_e", "T_r", "T_s", "op_a", "op_s", "f", "emission_E", "census_E", "source_E", "T_r_diag")}
         self.cells = _Cells(*[_dptr(self.arr[n]) for n, _ in _Cells._fields_])
-        lib().bo_initialize_cells(C.byref(self.mesh), C.byref(self.cells))
+        self.L.bo_initialize_cells(C.byref(self.mesh), C.byref(self.cells))
         self.census = np.zeros(0, PHOTON_DTYPE)
         # IMC_State time stepping (src/imc_state.h:42-45, :112-134, :292-296)
         self.time = deck.t_start
@@ -201,7 +232,7 @@ class Oracle:
 
     def source(self, step: int):
         """Energies and the photon list of one step (driver :54-75)."""
-        L = lib()
+        L = self.L
         d = self.deck
         en = _Energy()
         L.bo_calculate_photon_energy(C.byref(self.mesh), C.byref(self.cells), step, self.dt, C.byref(en))
@@ -219,7 +250,7 @@ class Oracle:
 
     def transport(self, photons: np.ndarray, next_dt: float, n_threads: Optional[int] = None):
         """replicated_transport's CPU history branch (replicated_transport.h:88-92)."""
-        L = lib()
+        L = self.L
         abs_E = np.zeros(self.n_cells)
         track_E = np.zeros(self.n_cells)
         t0 = time.perf_counter()
@@ -242,7 +273,7 @@ class Oracle:
         w = np.ascontiguousarray(w, dtype=np.float64)
         grad = np.zeros(self.n_cells)
         start = np.ascontiguousarray(start)
-        bad = lib().bo_adjoint_replay(C.byref(self.mesh), C.byref(self.cells), self.deck.seed, start.ctypes.data,
+        bad = self.L.bo_adjoint_replay(C.byref(self.mesh), C.byref(self.cells), self.deck.seed, start.ctypes.data,
                                       len(start), _dptr(w), int(scale), float(visit_bound), _dptr(grad),
                                       self.n_threads if n_threads is None else n_threads)
         return grad, int(bad)
@@ -254,9 +285,20 @@ class Oracle:
         op_a_p = np.ascontiguousarray(op_a_p, dtype=np.float64)
         f_p = np.ascontiguousarray(f_p, dtype=np.float64)
         start = np.ascontiguousarray(start)
-        return float(lib().bo_adjoint_reweighted(C.byref(self.mesh), C.byref(self.cells), _dptr(op_a_p),
+        return float(self.L.bo_adjoint_reweighted(C.byref(self.mesh), C.byref(self.cells), _dptr(op_a_p),
                                                  _dptr(f_p), self.deck.seed, start.ctypes.data, len(start),
                                                  _dptr(w)))
+
+    def trace(self, start_record: np.ndarray, max_segments: int = 1 << 16):
+        """transport_photon on one photon (a PHOTON_DTYPE record) with the
+        cell state of the current step: (per-segment TRACE_DTYPE records,
+        end record)."""
+        rec = np.ascontiguousarray(np.asarray(start_record, dtype=PHOTON_DTYPE).reshape(1))
+        out = np.zeros(max_segments, TRACE_DTYPE)
+        end = np.zeros(1, PHOTON_DTYPE)
+        n = self.L.bo_trace_photon(C.byref(self.mesh), C.byref(self.cells), self.deck.seed, rec.ctypes.data,
+                                   out.ctypes.data, max_segments, end.ctypes.data)
+        return out[:min(n, max_segments)].copy(), end[0]
 
     def fleck(self, op_a: np.ndarray, dt: float) -> np.ndarray:
         """Fleck factor per cell for the given opacities at the current
@@ -268,7 +310,7 @@ class Oracle:
         return 1.0 / (1.0 + dt * op_a * C_LIGHT * (4.0 * 0.01372 * T ** 3.0 / (cv * rho)))
 
     def step(self) -> StepResult:
-        L = lib()
+        L = self.L
         step = self.step_no
         en, photons = self.source(step)
         pre_census_E = float(np.sum(self.census["E"]))

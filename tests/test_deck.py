@@ -7,7 +7,7 @@ import pytest
 
 from branson_gb300 import deck as D
 
-REF = "/root/reference"
+REF = os.environ.get("BRANSON_REFERENCE", "/root/reference")
 
 
 def test_roundtrip_all_generators():

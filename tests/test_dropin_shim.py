@@ -8,7 +8,7 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference/src"
+REF = os.path.join(os.environ.get("BRANSON_REFERENCE", "/root/reference"), "src")
 
 
 @pytest.mark.skipif(not os.path.isdir(REF), reason="upstream checkout not present")
