@@ -14,15 +14,31 @@ value     histories transported / device time of K steps (CUDA events on the
 e2e       the same metric through the drop-in call bgs_replicated_transport
           on pinned host buffers, copies in the timed region
 roofline  k_transport_history: algorithmic bytes per launch / its CUDA-event
-          duration against the measured HBM copy bandwidth
+          duration against the measured HBM copy bandwidth.  The bytes are
+          96 B per census photon carried in and per census photon left
+          (pos 24, dir 24, E 8, E0 8, life 8, cell 4, group 4, counter 8,
+          stream 8) plus 104 B per cell (72 B of geometry and coefficients
+          read, 32 B of tallies written); photons made this step are
+          sourced from (cell, stream) and count 0 input bytes.
+roofline_history_bytes  the same kernel against a history-level byte
+          model: every history's 96-byte state read once and written once
+          (192 B per history) plus 104 B per cell
 roofline_issue  the same kernel's live segments/s times ncu's thread
-          instructions per segment, against the SM issue peak (the kernel
-          is integer-ALU / FP64 bound, not HBM bound)
+          instructions per segment, against the SM issue peak, and its FP64
+          instructions per segment against two FP64 lanes per clock per SM
+          (the kernel is integer-ALU / FP64 bound, not HBM bound)
 cpu_baseline  the oracle (C restatement, OpenMP on every host core) on a
-          bounded sample of the same deck, histories / transport time
+          bounded sample of the same deck at the same photons per step,
+          histories / transport time
+marshak, hohlraum  the other two plain decks at their own sizes (100-cell
+          Marshak wave at 1e6 photons over its 50 steps; 60^3 30-group
+          hohlraum at 5e7 photons over its 5 steps): GPU histories/s and
+          segments/s over whole device steps, and the oracle on the same
+          steps on the host cores
 
 --impl reference runs the CPU implementation (the oracle port of the
-upstream history loop, all host threads) on the same workload and metric.
+upstream history loop, all host threads) on the same workload, photons per
+step and steps, and reports the same metric.
 Multi-GPU (torchrun): independent replicas, one per GPU (weak scaling).
 """
 from __future__ import annotations
@@ -41,12 +57,15 @@ sys.path.insert(0, ROOT)
 
 METRIC = "histories/s on 1 GB300 (plain vs batched); adjoint/forward time at 1% tally err"
 UNIT = "histories/s"
-# algorithmic bytes of k_transport_history per launch: each history's state
-# read once and written once (96 B each way: pos 24, dir 24, E 8, E0 8,
-# life 8, cell 4, group 4, counter 8, stream 8) plus per cell 72 B of
-# coefficients/geometry read and 32 B of tallies written
-BYTES_PER_HISTORY = 192
+# algorithmic bytes of k_transport_history per launch: 96 B per census
+# photon carried in and per census photon left (pos 24, dir 24, E 8, E0 8,
+# life 8, cell 4, group 4, counter 8, stream 8), per cell 72 B of
+# coefficients/geometry read and 32 B of tallies written; photons made this
+# step are sourced from (cell, stream) and count 0 input bytes
+BYTES_PER_CENSUS_PHOTON = 96
 BYTES_PER_CELL = 104
+# the history-level model beside it: every history's state read and written
+BYTES_PER_HISTORY = 192
 
 
 def parse():
@@ -60,14 +79,14 @@ def parse():
     p.add_argument("--side", type=int, default=None)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--cpu-photons", type=float, default=1e6)
+    p.add_argument("--no-decks", action="store_true", help="skip the Marshak and hohlraum sections")
     p.add_argument("--no-adjoint", action="store_true")
     p.add_argument("--no-tune", action="store_true")
     p.add_argument("--no-batch", action="store_true")
     p.add_argument("--batch-problems", type=int, default=256)
     p.add_argument("--batch-photon-scale", type=float, default=1.0,
                    help="scale of the ensemble's photon counts (profiling small cases)")
-    p.add_argument("--only", choices=["main", "adjoint", "batch"], default=None,
+    p.add_argument("--only", choices=["main", "adjoint", "batch", "decks"], default=None,
                    help="run one section alone and print its JSON (profiling)")
     p.add_argument("--adjoint-photons", type=float, default=1e7)
     return p.parse_args()
@@ -113,12 +132,12 @@ class Clocks:
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index: int):
+        import tempfile
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{index}.csv")
+        self.path = os.path.join(tempfile.mkdtemp(prefix="bgs_clocks_"), f"clocks_gpu{index}.csv")
 
     def start(self):
-        os.makedirs(os.path.dirname(self.path), exist_ok=True)
         try:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
@@ -193,60 +212,52 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def cpu_port_rate(dk_gpu, photons: float, threads: int, steps: int = 1, warmup: int = 0):
+def cpu_port_rate(dk_gpu, threads: int, steps: int = 1, warmup: int = 0):
     """Oracle (C port of the upstream history loop) on the host cores, timed
-    over `steps` steps after `warmup` untimed ones (the GPU arm's steps)."""
+    over `steps` steps after `warmup` untimed ones, on the GPU arm's deck
+    (same photons per step).  Returns (histories, transport seconds,
+    segments, wall seconds)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import copy
     import oracle as O
-    dk = copy.deepcopy(dk_gpu)
-    dk.photons = int(photons)
-    orc = O.Oracle(dk, n_threads=threads)
+    orc = O.Oracle(copy.deepcopy(dk_gpu), n_threads=threads)
     for _ in range(warmup):
         orc.step()
     hist = 0
     secs = 0.0
     segs = 0
+    t0 = time.perf_counter()
     for _ in range(steps):
         r = orc.step()
         hist += len(r.source)
         secs += r.transport_s
         segs += r.segments
-    return hist, secs, segs
+    return hist, secs, segs, time.perf_counter() - t0
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the oracle port of the upstream CPU history path
+    (history_cpu_transport_photons over OpenMP, replicated_transport.h:88-92)
+    on every host thread, on the GPU arm's deck, photons per step and steps:
+    `warmup` untimed steps, then `steps` timed ones; histories / the sum of
+    the steps' transport times (the upstream transport timer,
+    replicated_transport.h:63-143, which leaves out sourcing)."""
     if rank != 0:
         return
     dk, cfg = make_deck(args)
     threads = os.cpu_count() or 1
-    photons = args.cpu_photons
-    cfg = dict(cfg, photons_per_step=int(photons), sample="photons per step reduced to fit minutes")
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import copy
-    import oracle as O
-    d2 = copy.deepcopy(dk)
-    d2.photons = int(photons)
-    orc = O.Oracle(d2, n_threads=threads)
-    for _ in range(args.warmup):
-        orc.step()
-    hist, secs = 0, 0.0
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        r = orc.step()
-        hist += len(r.source)
-        secs += r.transport_s
-    wall = time.perf_counter() - t0
+    hist, secs, segs, wall = cpu_port_rate(dk, threads, steps=args.steps, warmup=args.warmup)
     v = hist / secs
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": cfg, "impl": "reference",
+            "config": dict(cfg, parallelism=f"replicas{world}"), "impl": "reference",
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{args.steps} steps of the deck at {int(photons)} photons/step; "
-                                       f"transport time only (replicated_transport timer)"},
+                             "sample": f"steps {args.warmup + 1}-{args.warmup + args.steps} of the deck at "
+                                       f"{dk.photons} photons/step (after {args.warmup} untimed), "
+                                       f"{hist} histories, transport time only (replicated_transport timer)"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "wall_s": wall}
+            "segments_per_s": segs / secs, "wall_s": wall}
     print(json.dumps(line), flush=True)
 
 
@@ -283,8 +294,9 @@ def run_ours(args, rank, world, local):
         tuning = {"schedule": res.best.label(), "transport_ms": res.best_ms, "algorithm": imc.algorithm,
                   "candidates": {c.label(): ms for c, ms in res.timings}}
 
+    census_in = 0
     for _ in range(args.warmup):
-        imc.step(sync=True)
+        census_in = imc.step(sync=True).n_census
     barrier()
     torch.cuda.synchronize()
     clocks = Clocks(dev)
@@ -294,14 +306,15 @@ def run_ours(args, rank, world, local):
     ev1 = torch.cuda.Event(enable_timing=True)
     hist = 0
     segs = 0
-    transport_ms = []
+    transport_ms = []  # per step: (kernel ms, histories, census in, census out)
     ev0.record(stream)
     for _ in range(args.steps):
         r = imc.step(sync=True)
         hist += r.n_transported
         segs += r.n_segments
         ms, _k = imc.last_transport_ms()
-        transport_ms.append((ms, r.n_transported))
+        transport_ms.append((ms, r.n_transported, census_in, r.n_census))
+        census_in = r.n_census
     ev1.record(stream)
     torch.cuda.synchronize()
     barrier()
@@ -312,9 +325,11 @@ def run_ours(args, rank, world, local):
     value = hist_all / elapsed
 
     # roofline of the dominant kernel (k_transport_history), live CUDA events
-    k_ms = sum(m for m, _ in transport_ms) / len(transport_ms)
-    k_hist = sum(n for _, n in transport_ms) / len(transport_ms)
-    alg_bytes = BYTES_PER_HISTORY * k_hist + BYTES_PER_CELL * dk.n_cells
+    n_k = len(transport_ms)
+    k_ms = sum(t[0] for t in transport_ms) / n_k
+    k_hist = sum(t[1] for t in transport_ms) / n_k
+    k_census = sum(t[2] + t[3] for t in transport_ms) / n_k  # census photons in + out per launch
+    alg_bytes = BYTES_PER_CENSUS_PHOTON * k_census + BYTES_PER_CELL * dk.n_cells
     achieved = alg_bytes / (k_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peak_hbm()
     traffic = None
@@ -323,12 +338,20 @@ def run_ours(args, rank, world, local):
         with open(tpath) as fh:
             t = json.load(fh)
         traffic = t.get("bytes_per_history", 0) * k_hist + t.get("bytes_per_cell", 0) * dk.n_cells
-    seg_rate = segs / (sum(m for m, _ in transport_ms) * 1e-3)
+    seg_rate = segs / (sum(t[0] for t in transport_ms) * 1e-3)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs",
                 "kernel": "k_transport_history", "kernel_ms": k_ms, "segments_per_s": seg_rate,
-                "note": "integer-ALU / FP64-issue bound: the HBM fraction is small by construction; "
-                        "see roofline_issue"}
+                "algorithmic_bytes_per_launch": alg_bytes, "census_photons_in_plus_out_per_launch": k_census,
+                "note": "96 B per census photon in and out plus 104 B per cell; the kernel is integer-ALU / "
+                        "FP64-issue bound, so the HBM fraction is small by construction (roofline_issue "
+                        "holds the binding roof); traffic is ncu's DRAM bytes per history on the 1e6-photon "
+                        "case of the same deck, scaled to this launch's histories"}
+    hist_bytes = BYTES_PER_HISTORY * k_hist + BYTES_PER_CELL * dk.n_cells
+    roofline_hist = {"bound": "hbm", "achieved": hist_bytes / (k_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": hist_bytes / (k_ms * 1e-3) / 1e9 / peak, "bytes_per_launch": hist_bytes,
+                     "note": "every history's 96-byte state read and written once (192 B per history) plus "
+                             "104 B per cell"}
     roofline_issue = issue_roofline(seg_rate, clk, tpath)
 
     # end to end through the drop-in call on pinned host buffers
@@ -339,10 +362,11 @@ def run_ours(args, rank, world, local):
     cpu = None
     if not args.no_cpu_baseline and rank == 0 and world == 1:
         threads = os.cpu_count() or 1
-        h, s, sg = cpu_port_rate(dk, args.cpu_photons, threads, steps=1, warmup=args.warmup)
+        w = min(args.warmup, 2)
+        h, s, sg, _ = cpu_port_rate(dk, threads, steps=2, warmup=w)
         cpu = {"value": h / s, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"step {args.warmup + 1} (after {args.warmup} untimed, as the GPU arm) of the same "
-                         f"deck at {int(args.cpu_photons)} photons ({h} histories), transport time"}
+               "sample": f"steps {w + 1}-{w + 2} (after {w} untimed) of the same deck at {dk.photons} photons/step "
+                         f"({h} histories), transport time only; the reference arm runs the GPU arm's own steps"}
     imc.close()
     adjoint = None
     if not args.no_adjoint and rank == 0 and world == 1:
@@ -350,15 +374,20 @@ def run_ours(args, rank, world, local):
     batched = None
     if not args.no_batch and rank == 0 and world == 1:
         batched = batch_bench(args, dev)
+    decks = None
+    if not args.no_decks and rank == 0 and world == 1 and args.workload == "hot_zone":
+        decks = decks_bench(dev)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": dict(cfg, parallelism=f"replicas{world}"), "roofline": roofline,
-                "roofline_issue": roofline_issue,
+                "roofline_history_bytes": roofline_hist, "roofline_issue": roofline_issue,
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
                 "segments_per_s": segs / elapsed * world, "histories_per_step": hist / args.steps,
                 "tuning": tuning, "adjoint": adjoint, "batched": batched}
+        if decks:
+            line.update(decks)
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -394,6 +423,58 @@ def e2e_dropin(imc, dk, args):
         + 2 * 8 * dk.n_cells
     return {"value": hist / secs, "unit": UNIT, "h2d_bytes_per_step": int(in_bytes),
             "d2h_bytes_per_step": int(out_bytes), "call": "bgs_replicated_transport", "steps": k}
+
+
+def deck_rate(dk, dev, cfg, cpu_steps=None):
+    """One plain deck over all of its steps on the GPU (device time of the
+    whole steps, CUDA events on the context's stream, after one untimed
+    step of a separate context as warm-up), and the oracle over the same
+    steps (or the first `cpu_steps` of them) on every host core."""
+    import copy
+    import torch
+    from branson_gb300.engine import ReplicatedIMC
+    n_steps = int(round((dk.t_stop - dk.t_start) / dk.dt_start))
+    with ReplicatedIMC(copy.deepcopy(dk), device=dev) as w:
+        w.step(sync=True)
+    stream = torch.cuda.Stream(device=dev)
+    hist = segs = 0
+    with ReplicatedIMC(copy.deepcopy(dk), device=dev, stream=stream.cuda_stream) as imc:
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        kms = 0.0
+        for _ in range(n_steps):
+            r = imc.step(sync=True)
+            hist += r.n_transported
+            segs += r.n_segments
+            kms += imc.last_transport_ms()[0]
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        el = ev0.elapsed_time(ev1) / 1e3
+    threads = os.cpu_count() or 1
+    cs = n_steps if cpu_steps is None else cpu_steps
+    h, s, sg, wall = cpu_port_rate(dk, threads, steps=cs, warmup=0)
+    return dict(cfg, steps=n_steps, histories=int(hist), segments=int(segs), gpu_s=el, transport_kernel_s=kms / 1e3,
+                histories_per_s=hist / el, segments_per_s=segs / el,
+                cpu={"histories_per_s": h / s, "segments_per_s": sg / s, "cores": threads, "kind": "port",
+                     "steps": cs, "histories": int(h), "transport_s": s, "wall_s": wall,
+                     "sample": "the same deck and photons per step from step 1, transport time only"},
+                gpu_over_cpu=(hist / el) / (h / s))
+
+
+def decks_bench(dev):
+    """The other two plain decks at their own sizes: the 100-cell Marshak
+    wave at 1e6 photons over its 50 steps, and the 60^3 30-group hohlraum at
+    5e7 photons over its 5 steps (the oracle over its first 2)."""
+    from branson_gb300 import deck as D
+    m = D.marshak_wave(n_cells=100, photons=1_000_000, n_steps=50)
+    h = D.hohlraum(n_per_axis=60, photons=50_000_000, n_steps=5, n_groups=30)
+    return {"marshak": deck_rate(m, dev, {"workload": "marshak_100x1x1", "cells": 100, "photons_per_step": 1_000_000,
+                                          "dt": 0.001, "groups": 1, "seed": m.seed}),
+            "hohlraum": deck_rate(h, dev, {"workload": "hohlraum_60^3_30g", "cells": 216000,
+                                           "photons_per_step": 50_000_000, "dt": 0.005, "groups": 30,
+                                           "seed": h.seed}, cpu_steps=2)}
 
 
 def batch_adjoint_timing(b):
@@ -599,14 +680,14 @@ def adjoint_bench(args, dev, replicas: int = 6):
 def main():
     args = parse()
     rank, world, local = dist_env()
-    if args.only in ("adjoint", "batch"):
+    if args.only in ("adjoint", "batch", "decks"):
         import torch
         torch.cuda.set_device(0)
-        sect = adjoint_bench(args, 0) if args.only == "adjoint" else batch_bench(args, 0)
-        print(json.dumps({"section": args.only, args.only: sect}), flush=True)
+        fn = {"adjoint": adjoint_bench, "batch": batch_bench, "decks": lambda a, d: decks_bench(d)}[args.only]
+        print(json.dumps({"section": args.only, args.only: fn(args, 0)}), flush=True)
         return
     if args.only == "main":
-        args.no_adjoint = args.no_batch = True
+        args.no_adjoint = args.no_batch = args.no_decks = True
     if args.impl == "reference":
         run_reference(args, rank, world)
         return

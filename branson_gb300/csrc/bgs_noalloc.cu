@@ -20,6 +20,9 @@
 // Set-up: the first call on a device looks up the array's device address
 // with cudaGetSymbolAddress (once per device, with that device current), so
 // the first call on each device must come before any stream capture.
+// Every call is synchronous: it enqueues its work on the caller's stream,
+// copies the device checks' flags back into host memory and waits for the
+// stream before it returns.
 // Every call shares the one array: the tallies and counters are cleared at
 // the start of each call, and two calls whose work overlaps on the GPU (on
 // different streams, or from different host threads) race on it.

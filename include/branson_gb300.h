@@ -220,8 +220,9 @@ BGS_API int bgs_replicated_transport(bgs_context *ctx, uint64_t n, const bgs_pho
  * 11 MB) is held by every GPU that loads the library until exit.  The first
  * call on a device looks up the array's address, so it must come before
  * any stream capture.  All calls share the array: calls that overlap on the
- * GPU race.  Returns after the work completes (BGS_ERR_DEVICE if a device
- * check fired). */
+ * GPU race.  Each call is synchronous: it enqueues its work on `stream`,
+ * copies the device checks' flags to host memory and waits for the stream,
+ * returning BGS_ERR_DEVICE if a check fired. */
 BGS_API int bgs_transport_device_noalloc(uint32_t ngx, uint32_t ngy, uint32_t ngz, uint32_t n_groups,
                                          const double *x_planes, const double *y_planes,
                                          const double *z_planes, const int32_t bc[6], const double *op_a,

@@ -3,9 +3,10 @@
 // through the C ABI in branson_gb300.h.
 //
 // Use: in the Branson tree, include this header instead of
-// "replicated_transport.h" (src/replicated_driver.h:191), or define
-// BRANSON_GB300_TRANSPORT and include it after the upstream headers; link
-// against libbranson_gb300.so.  imc_replicated_driver is unchanged: it calls
+// "replicated_transport.h" (the include at src/replicated_driver.h:28), or
+// define BRANSON_GB300_TRANSPORT and include it after the upstream headers;
+// link against libbranson_gb300.so.  imc_replicated_driver is unchanged: it
+// calls (src/replicated_driver.h:87-88)
 //
 //   census = replicated_transport<Census_T>(mesh, gpu_setup, imc_state,
 //                abs_E, track_E, all_photons, n_omp_threads, batch_size,
@@ -25,8 +26,14 @@
 //
 // One device context per process (the replicated mesh is uploaded on the
 // first call; opacities and Fleck factors are uploaded every call).  The
-// header needs the upstream types (Mesh, Cell, Photon, PhotonArray, RNG,
-// IMC_State, GPU_Setup, Timer) to be declared before it is included.
+// photon banks are sized for twice the first call's list; a later, longer
+// list (census growth over steps) replaces the context with one twice its
+// length.  Only group 0's absorption and scattering opacities are uploaded:
+// the upstream cells set every group to the same value (Cell::set_op_a /
+// set_op_s, cell.h:260-275), and the device tables keep one opacity per cell
+// with the group drawn uniformly.  The header needs the upstream types (Mesh,
+// Cell, Photon, PhotonArray, RNG, IMC_State, GPU_Setup, Timer) to be
+// declared before it is included.
 #ifndef BRANSON_GB300_TRANSPORT_HPP
 #define BRANSON_GB300_TRANSPORT_HPP
 
@@ -69,6 +76,7 @@ inline RNG rng_from(uint64_t seed_hi, uint64_t stream, uint64_t counter) {
 struct Context {
   bgs_context *ctx = nullptr;
   uint64_t seed_hi = 0;
+  uint64_t capacity = 0;  // photons per device bank
   uint32_t n_cells = 0;
   std::vector<double> x, y, z;
   std::vector<double> op_a, op_s, f;
@@ -111,11 +119,16 @@ inline void upload_mesh(Context &C, const Mesh &mesh) {
 
 inline Context &context(const Mesh &mesh, size_t n_photons, uint64_t seed_hi) {
   static Context C;
+  if (C.ctx && (uint64_t)n_photons > C.capacity) {  // a longer list than the banks hold: a new context
+    check(C.ctx, bgs_destroy(C.ctx), "bgs_destroy");
+    C.ctx = nullptr;
+  }
   if (!C.ctx) {
     const uint64_t cap = 2 * (uint64_t)n_photons + 4096;
     check(nullptr, bgs_create(&C.ctx, 0, cap, nullptr, (uint32_t)(seed_hi >> 32), 0), "bgs_create");
     upload_mesh(C, mesh);
     C.seed_hi = seed_hi;
+    C.capacity = cap;
   }
   return C;
 }
