@@ -82,3 +82,42 @@ def test_fixed_point_sums_do_not_depend_on_threads():
     g1, _ = orc.adjoint(start, w, scale, bound, n_threads=1)
     g4, _ = orc.adjoint(start, w, scale, bound, n_threads=4)
     np.testing.assert_array_equal(g1, g4)
+
+
+def test_cutoff_jump_is_the_only_bias():
+    """The estimator does not differentiate the E/E0 < 0.01 cutoff
+    (photon.h:47-49): a history crossing it gives up its last 1% at once, a
+    jump of 0.01 E0 in the tally that a pathwise derivative cannot see.  On
+    a one-cell pure absorber (T_e = 0, so f = 1 and no effective scattering;
+    census photons only, whose counts and weights do not depend on sigma_a)
+    every history is one straight flight of length d to a face, killed when
+    sigma_a d > ln 100.  The common-random-number central difference of the
+    oracle's tally then exceeds the replayed gradient by exactly the counted
+    jumps, sum over crossing photons of 0.01 E0 / (2 h sigma_a)."""
+    from branson_gb300.deck import Deck, Division, Region, VACUUM
+    dk = Deck(t_start=0.0, t_stop=0.01, dt_start=0.01, t_mult=1.0, dt_max=1.0, photons=200000, seed=21,
+              x_divisions=[Division(0.0, 1.0, 1)], y_divisions=[Division(0.0, 1.0, 1)],
+              z_divisions=[Division(0.0, 1.0, 1)], region_map={(0, 0, 0): 1}, bc=(VACUUM,) * 6, T_source=0.0,
+              regions=[Region(1, 0.1, 1.0, 5.0, 0.0, 0.0, 0.0, 0.0, 0.5)])
+    orc, start, _, segs = _run(dk, n_threads=4)
+    assert orc.arr["f"][0] == 1.0 and np.all(start["source_type"] == 0)
+    sig, nd = orc.arr["op_a"][0], orc.dt
+    w = np.ones(1)
+    scale, bound = O.adjoint_scale(w, start, orc.arr["op_a"], orc.arr["op_s"], orc.arr["f"], segs)
+    grad, dropped = orc.adjoint(start, w, scale, bound)
+    assert dropped == 0
+
+    def tally(s):
+        orc.arr["op_a"][:] = s
+        a, *_ = orc.transport(start.copy(), nd)
+        orc.arr["op_a"][:] = sig
+        return a.sum()
+
+    pos, d = start["pos"], start["dir"]
+    flight = np.where(d > 0, (1.0 - pos) / d, -pos / d).min(axis=1)  # to the first face
+    for h in (3e-3, 1e-3):
+        fd = (tally(sig * (1 + h)) - tally(sig * (1 - h))) / (2 * h * sig)
+        cross = (sig * (1 - h) * flight < np.log(100.0)) & (np.log(100.0) < sig * (1 + h) * flight)
+        jumps = 0.01 * start["E0"][cross].sum() / (2 * h * sig)
+        assert cross.sum() > 50
+        assert abs((fd - grad[0]) - jumps) <= 0.01 * jumps, (h, fd, grad[0], jumps)
