@@ -80,6 +80,10 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-decks", action="store_true", help="skip the Marshak and hohlraum sections")
+    p.add_argument("--algorithm", choices=["tuned", "history", "event"], default="tuned",
+                   help="transport algorithm of the main section (history/event: no tuning)")
+    p.add_argument("--comb", type=int, default=0,
+                   help="comb the census to at most this many photons after every step (comb_photons)")
     p.add_argument("--no-adjoint", action="store_true")
     p.add_argument("--no-tune", action="store_true")
     p.add_argument("--no-batch", action="store_true")
@@ -89,6 +93,8 @@ def parse():
     p.add_argument("--only", choices=["main", "adjoint", "batch", "decks"], default=None,
                    help="run one section alone and print its JSON (profiling)")
     p.add_argument("--adjoint-photons", type=float, default=1e7)
+    p.add_argument("--no-fd-check", action="store_true",
+                   help="adjoint section: time the forward/backward pair only (profiling)")
     return p.parse_args()
 
 
@@ -288,15 +294,28 @@ def run_ours(args, rank, world, local):
     # (block size, histories per thread, history vs event mode; results are
     # identical under every schedule)
     tuning = None
-    if not args.no_tune:
+    if args.algorithm != "tuned":
+        imc.algorithm = _lib.HISTORY if args.algorithm == "history" else _lib.EVENT
+    elif not args.no_tune:
         from branson_gb300.tune import tune
         res = tune(imc, repeats=2)
         tuning = {"schedule": res.best.label(), "transport_ms": res.best_ms, "algorithm": imc.algorithm,
                   "candidates": {c.label(): ms for c, ms in res.timings}}
 
+    comb_ctr = 0
+
+    def comb(n_census):
+        # census population control between steps (census_functions.h:48-93),
+        # RNG stream 2^62 (apart from every photon's), its counter carried on
+        nonlocal comb_ctr
+        if not args.comb:
+            return n_census
+        kept, comb_ctr = imc.comb_census(args.comb, stream=1 << 62, counter=comb_ctr)
+        return kept
+
     census_in = 0
     for _ in range(args.warmup):
-        census_in = imc.step(sync=True).n_census
+        census_in = comb(imc.step(sync=True).n_census)
     barrier()
     torch.cuda.synchronize()
     clocks = Clocks(dev)
@@ -314,7 +333,7 @@ def run_ours(args, rank, world, local):
         segs += r.n_segments
         ms, _k = imc.last_transport_ms()
         transport_ms.append((ms, r.n_transported, census_in, r.n_census))
-        census_in = r.n_census
+        census_in = comb(r.n_census)
     ev1.record(stream)
     torch.cuda.synchronize()
     barrier()
@@ -604,6 +623,8 @@ def adjoint_bench(args, dev, replicas: int = 6):
     tallies, grads, tapes_info = [], [], None
     tf, tb, fwd_kernel_ms = [], [], 0.0
     runs = []  # per replica: (context, tape, counts)
+    if args.no_fd_check:
+        replicas = 1
     for r in range(replicas):
         dk_r = D.random_opacity_cube(n_per_axis=32, photons=photons, seed=777)
         dk_r.seed = 777 + 1000 * r
@@ -624,6 +645,12 @@ def adjoint_bench(args, dev, replicas: int = 6):
         grads.append(g)
         runs.append((st, tape.counts()))
         tape.close()
+    if args.no_fd_check:
+        for st, _ in runs:
+            st.close()
+        fwd, bwd = statistics.median(tf), statistics.median(tb)
+        return {"histories": int(tapes_info["n_histories"]), "forward_ms": 1e3 * fwd, "backward_ms": 1e3 * bwd,
+                "backward_over_forward": bwd / fwd, "backward_replay_kernel_ms": tapes_info["replay_ms"]}
     T = np.array(tallies)
     mean = T.mean(axis=0)
     rel_err = np.where(mean > 0, T.std(axis=0, ddof=1) / np.where(mean > 0, mean, 1.0), np.inf)
