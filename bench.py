@@ -389,13 +389,13 @@ def run_ours(args, rank, world, local):
     imc.close()
     adjoint = None
     if not args.no_adjoint and rank == 0 and world == 1:
-        adjoint = adjoint_bench(args, dev)
+        adjoint = guarded(adjoint_bench, args, dev)
     batched = None
     if not args.no_batch and rank == 0 and world == 1:
-        batched = batch_bench(args, dev)
+        batched = guarded(batch_bench, args, dev)
     decks = None
     if not args.no_decks and rank == 0 and world == 1 and args.workload == "hot_zone":
-        decks = decks_bench(dev)
+        decks = guarded(decks_bench, dev)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
@@ -405,8 +405,10 @@ def run_ours(args, rank, world, local):
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
                 "segments_per_s": segs / elapsed * world, "histories_per_step": hist / args.steps,
                 "tuning": tuning, "adjoint": adjoint, "batched": batched}
-        if decks:
+        if decks and "error" not in decks:
             line.update(decks)
+        elif decks:
+            line["decks"] = decks
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -414,7 +416,12 @@ def run_ours(args, rank, world, local):
 
 
 def e2e_dropin(imc, dk, args):
-    """Drop-in replicated_transport on pinned host buffers, copies timed."""
+    """Drop-in replicated_transport on pinned host buffers, the host-device
+    traffic inside the timed region.  The buffers are page-locked and mapped
+    into the device, so by default the kernels read each photon's state at
+    pickup and write its end state in place over the host link (NVLink-C2C
+    on GB300); the same call with the zero_copy option off copies the bank
+    in and the end states out around a pipelined transport, timed beside it."""
     import numpy as np
     from branson_gb300._lib import PhotonArrays
     # inputs: the current step's photon list, made on the device and copied out
@@ -426,22 +433,31 @@ def e2e_dropin(imc, dk, args):
     work = PhotonArrays(n, pinned=True)
     census = PhotonArrays(n, pinned=True)
     nd = imc.next_dt() if imc.next_dt() > 0 else dt
-    hist, secs = 0, 0.0
     k = max(1, min(args.steps, 3))
-    for it in range(k + 1):
-        for name in work.arrays:
-            np.copyto(work[name], src[name])
-        t0 = time.perf_counter()
-        abs_E, trk_E, cen, ce, ex = imc.replicated_transport(work, nd, census=census)
-        t1 = time.perf_counter()
-        if it > 0:  # first call is warm-up
-            hist += n
-            secs += t1 - t0
+    rates = {}
+    for zero_copy in (1, 0):
+        imc.set_option("zero_copy", zero_copy)
+        hist, secs = 0, 0.0
+        for it in range(k + 1):
+            for name in work.arrays:
+                np.copyto(work[name], src[name])
+            t0 = time.perf_counter()
+            abs_E, trk_E, cen, ce, ex = imc.replicated_transport(work, nd, census=census)
+            t1 = time.perf_counter()
+            if it > 0:  # first call is warm-up
+                hist += n
+                secs += t1 - t0
+        rates[zero_copy] = hist / secs
+    imc.set_option("zero_copy", 1)
     in_bytes = sum(a.nbytes for a in src.arrays.values())
     out_bytes = n * (6 * 8 + 8 + 8 + 4 + 4 + 1 + 8) + cen.n * sum(a.itemsize for a in src.arrays.values()) \
         + 2 * 8 * dk.n_cells
-    return {"value": hist / secs, "unit": UNIT, "h2d_bytes_per_step": int(in_bytes),
-            "d2h_bytes_per_step": int(out_bytes), "call": "bgs_replicated_transport", "steps": k}
+    return {"value": rates[1], "unit": UNIT, "h2d_bytes_per_step": int(in_bytes),
+            "d2h_bytes_per_step": int(out_bytes), "call": "bgs_replicated_transport", "steps": k,
+            "transfer": "photon state read at pickup and end states written in place by the kernels in "
+                        "page-locked mapped host memory (over NVLink-C2C); census and tallies copied out",
+            "copied_value": rates[0],
+            "copied_transfer": "bank copied in and end states out (cudaMemcpyAsync) around a pipelined transport"}
 
 
 def deck_rate(dk, dev, cfg, cpu_steps=None):
@@ -598,6 +614,31 @@ def batch_bench(args, dev, steps: int = 2):
             "timing": "host wall clock around each whole step (sync), same problems and results in both arms"}
 
 
+_RETRIES = {"fd_forward": 0}
+
+
+def fd_forward(st, sigma_a, counts):
+    """A finite-difference forward at frozen photon counts.  One retry after a
+    device check: an FD forward once raised the supplied-counts check in the
+    bench (not reproduced since); the retries are counted in the JSON."""
+    from branson_gb300._lib import BransonError
+    try:
+        return st.forward(sigma_a=sigma_a, counts=counts, save=False)[0]
+    except BransonError as e:
+        _RETRIES["fd_forward"] += 1
+        _RETRIES.setdefault("last_error", str(e))
+        return st.forward(sigma_a=sigma_a, counts=counts, save=False)[0]
+
+
+def guarded(fn, *a):
+    """A bench section whose failure is reported in its own key instead of
+    ending the run before the headline line is printed."""
+    try:
+        return fn(*a)
+    except Exception as e:  # reported, not hidden: the section's JSON holds the error
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
 def adjoint_bench(args, dev, replicas: int = 6):
     """Differentiation workload: 32^3 cube, one region per cell with sigma_a ~
     lognormal(ln 20, 0.5) from seed 777, T0 = 0.1 keV, 1 keV source on x-,
@@ -666,15 +707,15 @@ def adjoint_bench(args, dev, replicas: int = 6):
             sp, sm = sig0.copy(), sig0.copy()
             sp[j] *= 1 + h
             sm[j] *= 1 - h
-            ap, _ = st.forward(sigma_a=sp, counts=counts, save=False)
-            am, _ = st.forward(sigma_a=sm, counts=counts, save=False)
+            ap = fd_forward(st, sp, counts)
+            am = fd_forward(st, sm, counts)
             row.append(float(np.dot(w, ap - am) / (2 * h * sig0[j])))
         FD.append(row)
         sp, sm = sig0.copy(), sig0.copy()
         sp[cells] *= 1 + h * v
         sm[cells] *= 1 - h * v
-        ap, _ = st.forward(sigma_a=sp, counts=counts, save=False)
-        am, _ = st.forward(sigma_a=sm, counts=counts, save=False)
+        ap = fd_forward(st, sp, counts)
+        am = fd_forward(st, sm, counts)
         DIR_FD.append(float(np.dot(w, ap - am) / (2 * h)))
         st.close()
     FD = np.array(FD)
@@ -687,6 +728,11 @@ def adjoint_bench(args, dev, replicas: int = 6):
     dir_fd = np.array(DIR_FD)
     dir_diff = dir_adj - dir_fd
     fwd, bwd = statistics.median(tf), statistics.median(tb)
+    # the per-replica spread of each cell's difference, and the replicas a
+    # median standard error of 0.3% would take at this history count
+    sd1 = diff.std(axis=0, ddof=1) / np.abs(FD.mean(axis=0))
+    fd_s = 2 * len(cells) + 1  # forwards per replica
+    resolved_class = fd_check_resolved(args, dev)
     return {"workload": "random_opacity_cube 32^3, sigma_a ~ lognormal(ln 20, 0.5), 1 keV source on x-, "
                         f"{photons} photons, one step of 0.01 sh",
             "histories": int(tapes_info["n_histories"]), "segments": int(tapes_info["n_segments"]),
@@ -701,7 +747,62 @@ def adjoint_bench(args, dev, replicas: int = 6):
                          "frac_z_le_3": float(np.mean(z <= 3.0)) if len(z) else None,
                          "median_rel_stderr": float(np.median(se / np.abs(FD.mean(axis=0)))) if len(se) else None,
                          "directional_rel_diff": float(abs(dir_diff.mean()) / abs(dir_fd.mean())),
-                         "directional_rel_stderr": float(dir_diff.std(ddof=1) / math.sqrt(k) / abs(dir_fd.mean()))}}
+                         "directional_rel_stderr": float(dir_diff.std(ddof=1) / math.sqrt(k) / abs(dir_fd.mean())),
+                         "median_rel_sd_per_replica": float(np.median(sd1)) if len(sd1) else None,
+                         "replicas_for_0.3pct_median_stderr": int(math.ceil((np.median(sd1) / 0.003) ** 2))
+                         if len(sd1) else None,
+                         "forwards_per_replica": fd_s},
+            "fd_check_resolved": resolved_class, "fd_forward_retries": dict(_RETRIES)}
+
+
+def fd_check_resolved(args, dev, replicas: int = 16):
+    """The 1% criterion on a deck class that resolves it: a 4^3 cube (64
+    cells of 0.25 cm, every one checked) with the differentiation deck's
+    physics and sigma_a ~ lognormal(ln 2, 0.5), a tenth of the 32^3 deck's
+    law, so that no history decays to the E/E0 < 0.01 cutoff, whose jump the
+    estimator does not differentiate; 1e7 photons per replica, w ~ U(0,1).
+    Per cell: the mean over independent-seed replicas of the adjoint gradient
+    and of the CRN central difference (h = 1e-4 relative, counts frozen),
+    their difference relative to the FD mean, and its standard error."""
+    import numpy as np
+    from branson_gb300 import deck as D
+    from branson_gb300.adjoint import AdjointStep
+    n, photons, h = 4, int(args.adjoint_photons), 1e-4
+    make = lambda seed: D.random_opacity_cube(n_per_axis=n, photons=photons, seed=777, sigma_median=2.0)
+    dk = make(777)
+    sig0 = np.array([r.opacA for r in dk.regions])[dk.cell_regions()]
+    w = np.random.default_rng(777).uniform(0.0, 1.0, dk.n_cells)
+    adj, fd = [], []
+    t0 = time.perf_counter()
+    for r in range(replicas):
+        dk_r = make(777)
+        dk_r.seed = 777 + 1000 * r
+        with AdjointStep(dk_r, device=dev) as st:
+            _, tape = st.forward(sigma_a=sig0)
+            counts = tape.counts()
+            adj.append(st.backward(tape, w))
+            row = []
+            for j in range(dk.n_cells):
+                sp, sm = sig0.copy(), sig0.copy()
+                sp[j] *= 1 + h
+                sm[j] *= 1 - h
+                ap = fd_forward(st, sp, counts)
+                am = fd_forward(st, sm, counts)
+                row.append(float(np.dot(w, ap - am) / (2 * h * sig0[j])))
+            fd.append(row)
+            tape.close()
+    adj, fd = np.array(adj), np.array(fd)
+    d = adj - fd
+    scale = np.abs(fd.mean(axis=0))
+    rel = np.abs(d.mean(axis=0)) / scale
+    se = d.std(axis=0, ddof=1) / math.sqrt(replicas) / scale
+    return {"workload": f"random_opacity_cube {n}^3, sigma_a ~ lognormal(ln 2, 0.5), 1 keV source on x-, "
+                        f"{photons} photons, one step of 0.01 sh; all {dk.n_cells} cells",
+            "replicas": replicas, "h_rel": h, "seconds": time.perf_counter() - t0,
+            "median_rel_stderr": float(np.median(se)), "median_rel_diff": float(np.median(rel)),
+            "frac_within_1pct": float(np.mean(rel <= 0.01)),
+            "frac_within_1pct_plus_2se": float(np.mean(rel <= 0.01 + 2.0 * se)),
+            "max_rel_diff": float(rel.max()), "rel_stderr_at_max": float(se[int(np.argmax(rel))])}
 
 
 def main():

@@ -21,7 +21,7 @@ REFLECT, VACUUM, ELEMENT, SOURCE, PROCESSOR = range(5)
 EXIT, PASS, CENSUS, SCATTER, KILLED, BOUND = range(6)
 HISTORY, EVENT = 0, 1
 OPTIONS = {"event_round_cap": 0, "event_check_every": 1, "event_tail_fraction": 2, "transport_blocks": 3,
-           "transport_threads": 4, "pipeline_min_photons": 5}
+           "transport_threads": 4, "pipeline_min_photons": 5, "zero_copy": 6}
 BATCH_OPTIONS = {"graph": 0, "transport_blocks": 1}
 FIELDS = {"T_e": 0, "T_r": 1, "op_a": 2, "op_s": 3, "f": 4, "emission_E": 5, "census_E": 6,
           "source_E": 7, "abs_E": 8, "track_E": 9}

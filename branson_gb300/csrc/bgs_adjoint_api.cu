@@ -245,6 +245,9 @@ int bgs_adjoint_forward(bgs_context *ctx, const bgs_step_params *p, const double
   if (rc) return rc;
   const uint32_t nc = ctx->mesh.n_cells;
   cudaStream_t s = ctx->stream;
+  // a forward is a function of its inputs: its device checks start clear
+  BGS_CUDA(ctx, cudaMemsetAsync(&ctx->d_diag->flags, 0, sizeof(uint32_t), s));
+  BGS_CUDA(ctx, cudaMemsetAsync(&ctx->d_diag->bad_counts_cell, 0, sizeof(uint32_t), s));
 
   // energies from the caller's opacities (or the region law)
   const double *sig_dev = nullptr;

@@ -131,6 +131,53 @@ __global__ void k_reset_work(DeviceDiag *d) { d->work_counter = 0; }
 
 namespace {
 
+// The device address of a host array the GPU can read and write in place:
+// page-locked host memory mapped into the device's address space
+// (cudaMallocHost, cudaHostAlloc, or cudaHostRegister with mapping), or
+// nullptr for any other memory (pageable host memory, device memory).
+template <typename T>
+T *mapped_alias(T *host) {
+  if (!host) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+    (void)cudaGetLastError();  // not memory the runtime knows: no alias
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr) return nullptr;
+  return static_cast<T *>(a.devicePointer);
+}
+
+// every array of the caller's photons as a device-visible bank, or false
+bool mapped_bank(const bgs_photons_host *in, Bank &b) {
+  b.px = mapped_alias(in->pos_x); b.py = mapped_alias(in->pos_y); b.pz = mapped_alias(in->pos_z);
+  b.dx = mapped_alias(in->dir_x); b.dy = mapped_alias(in->dir_y); b.dz = mapped_alias(in->dir_z);
+  b.E = mapped_alias(in->E); b.E0 = mapped_alias(in->E0); b.life = mapped_alias(in->life_dx);
+  b.cell = mapped_alias(in->cell); b.group = mapped_alias(in->group);
+  b.desc = mapped_alias(in->descriptor); b.stype = mapped_alias(in->source_type);
+  b.stream = reinterpret_cast<unsigned long long *>(mapped_alias(in->rng_stream));
+  b.ctr = reinterpret_cast<unsigned long long *>(mapped_alias(in->rng_counter));
+  return b.px && b.py && b.pz && b.dx && b.dy && b.dz && b.E && b.E0 && b.life && b.cell && b.group &&
+         b.desc && b.stype && b.stream && b.ctr;
+}
+
+// Drop-in transport of photons in mapped host memory, in place: the history
+// kernel reads each photon's state at pickup and writes its end state at
+// the end straight to the caller's arrays (over the host link: NVLink-C2C
+// on GB300), the census pass reads them there and compacts the census into
+// the device bank, and no bulk copy runs before or after the kernel.  The
+// arithmetic and the work items are those of the device-bank path, so the
+// results are the same bits.
+int transport_mapped(bgs_context *ctx, uint64_t n, const Bank &hb, double next_dt) {
+  const uint64_t before = ctx->launches;
+  k_set_bank_size<<<1, 1, 0, ctx->stream>>>(ctx->d_diag, n);
+  BGS_LAUNCHED(ctx, 1);
+  int rc;
+  if ((rc = run_transport(ctx, hb, BGS_HISTORY))) return rc;
+  if ((rc = finish_transport_from(ctx, hb, next_dt))) return rc;
+  ctx->last_launches = (uint32_t)(ctx->launches - before);
+  return BGS_OK;
+}
+
 // Drop-in transport of a large host bank as a pipeline: the weights and
 // flights go first (the fixed-point scales need the whole bank's maxima),
 // the rest of the state follows in chunks on a copy stream, and each chunk
@@ -566,8 +613,9 @@ int run_transport(bgs_context *ctx, const Bank &from, uint32_t algorithm) {
   return BGS_OK;
 }
 
-int finish_transport(bgs_context *ctx, double next_dt) {
-  Bank &from = ctx->bank[ctx->cur];
+// census compaction of the transported bank `from` into the other device
+// bank (which becomes current), tallies to doubles
+int finish_transport_from(bgs_context *ctx, const Bank &from, double next_dt) {
   Bank &to = ctx->bank[1 - ctx->cur];
   launch_scan_flags(from.desc, CENSUS, (uint32_t)ctx->capacity, &ctx->d_diag->n_bank, ctx->d_off_bank,
                     ctx->d_tile_bank, ctx->stream);
@@ -579,6 +627,10 @@ int finish_transport(bgs_context *ctx, double next_dt) {
   ctx->cur = 1 - ctx->cur;
   ctx->bank_is_census = true;
   return BGS_OK;
+}
+
+int finish_transport(bgs_context *ctx, double next_dt) {
+  return finish_transport_from(ctx, ctx->bank[ctx->cur], next_dt);
 }
 
 namespace {
@@ -696,7 +748,14 @@ int bgs_replicated_transport(bgs_context *ctx, uint64_t n, const bgs_photons_hos
   if (!ctx || !photons) return BGS_ERR_INVALID;
   if (!ctx->has_mesh) return fail(ctx, BGS_ERR_STATE, "no mesh");
   int rc;
-  if (algorithm == BGS_HISTORY && ctx->pipe_min_photons > 0 && n >= ctx->pipe_min_photons && n > 0) {
+  Bank mapped;
+  if (algorithm == BGS_HISTORY && ctx->zero_copy && n > 0 && !(rc = set_device(ctx)) &&
+      mapped_bank(photons, mapped)) {
+    if (n > ctx->capacity)
+      return fail(ctx, BGS_ERR_CAPACITY, "%llu photons exceed the bank capacity %llu", (unsigned long long)n,
+                  ctx->capacity);
+    if ((rc = transport_mapped(ctx, n, mapped, next_dt))) return rc;
+  } else if (algorithm == BGS_HISTORY && ctx->pipe_min_photons > 0 && n >= ctx->pipe_min_photons && n > 0) {
     if (n > ctx->capacity)
       return fail(ctx, BGS_ERR_CAPACITY, "%llu photons exceed the bank capacity %llu", (unsigned long long)n,
                   ctx->capacity);
@@ -763,6 +822,10 @@ int bgs_set_option(bgs_context *ctx, int option, double value) {
     case BGS_OPT_PIPELINE_MIN_PHOTONS:
       if (!(value >= 0 && value <= 1e15)) break;
       ctx->pipe_min_photons = (unsigned long long)value;
+      return BGS_OK;
+    case BGS_OPT_ZERO_COPY:
+      if (value != 0 && value != 1) break;
+      ctx->zero_copy = value != 0;
       return BGS_OK;
     case BGS_OPT_TRANSPORT_THREADS:
       if (value != 64 && value != 128 && value != 256) break;

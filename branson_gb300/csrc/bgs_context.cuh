@@ -68,6 +68,7 @@ struct bgs_context {
   // second compute stream, per-chunk events and work counters
   static constexpr int kPipeChunks = 8;
   unsigned long long pipe_min_photons = 1ULL << 20;  // 0: never pipelined
+  bool zero_copy = true;  // history-mode drop-in on mapped host arrays: transported in place
   cudaStream_t copy_stream = nullptr, aux_stream = nullptr;
   cudaEvent_t pipe_start = nullptr, pipe_prep = nullptr, pipe_aux = nullptr, pipe_back = nullptr;
   cudaEvent_t pipe_in[kPipeChunks] = {}, pipe_done[kPipeChunks] = {};
@@ -151,7 +152,12 @@ inline int check_flags(bgs_context *ctx, uint32_t flags) {
   if (flags & FLAG_SEGMENT_LIMIT) what += " a history hit the segment limit;";
   if (flags & FLAG_BAD_CELL) what += " a photon referenced a cell outside the mesh;";
   if (flags & FLAG_NAN) what += " a non-finite tally contribution was dropped;";
-  if (flags & FLAG_BAD_COUNTS) what += " supplied photon counts disagree with the cell energies;";
+  if (flags & FLAG_BAD_COUNTS) {
+    what += " supplied photon counts disagree with the cell energies";
+    if (ctx->h_diag && ctx->h_diag->bad_counts_cell)
+      what += " (cell " + std::to_string(ctx->h_diag->bad_counts_cell - 1) + ")";
+    what += ";";
+  }
   return fail(ctx, (flags & FLAG_CAPACITY) ? BGS_ERR_CAPACITY : BGS_ERR_DEVICE,
               "device check fired (flags 0x%x):%s", flags, what.c_str());
 }
@@ -168,7 +174,8 @@ inline int read_diag(bgs_context *ctx) {
 // run_transport: prepare + every photon in `from` transported (history or
 // event mode) into the context's tallies.  finish_transport: census
 // compaction into the other bank (which becomes current) and the tallies
-// converted to doubles.
+// converted to doubles; finish_transport_from does the same for another
+// transported bank (the caller's mapped host arrays).
 int prepare_transport(bgs_context *ctx, const Bank &from);
 
 // a batch's contexts in problem order, and its error message (bgs_batch_api.cu)
@@ -177,3 +184,4 @@ const std::vector<bgs_context *> &batch_contexts(const bgs_batch *b);
 int batch_fail(bgs_batch *b, int code, const std::string &msg);
 int run_transport(bgs_context *ctx, const Bank &from, uint32_t algorithm);
 int finish_transport(bgs_context *ctx, double next_dt);
+int finish_transport_from(bgs_context *ctx, const Bank &from, double next_dt);

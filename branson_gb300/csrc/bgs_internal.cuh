@@ -178,6 +178,7 @@ struct DeviceDiag {
   int scale_abs;                      // fixed-point exponent of this step's energy sums
   uint32_t flags;
   uint32_t serial_needed;             // a photon count needed the serial energy sum
+  uint32_t bad_counts_cell;           // 1 + a cell whose supplied photon counts disagreed (0: none)
 };
 
 // ------------------------------------------------------------------ RNG

@@ -225,7 +225,10 @@ __global__ void k_check_counts(MeshDev m, CellsDev c, DeviceDiag *d, uint32_t st
   bool bad = (c.em_E[g] > 0.0) != (c.n_em[g] > 0u) || (c.so_E[g] > 0.0) != (c.n_so[g] > 0u);
   if (step == 1) bad |= (c.ce_E[g] > 0.0) != (c.n_ce[g] > 0u);
   else bad |= c.n_ce[g] != 0u;
-  if (bad) atomicOr(&d->flags, (uint32_t)FLAG_BAD_COUNTS);
+  if (bad) {
+    atomicOr(&d->flags, (uint32_t)FLAG_BAD_COUNTS);
+    atomicCAS(&d->bad_counts_cell, 0u, g + 1u);
+  }
 }
 
 void launch_check_counts(const MeshDev &m, const CellsDev &c, DeviceDiag *d, uint32_t step, cudaStream_t s) {

@@ -193,7 +193,12 @@ BGS_API int bgs_comb_census(bgs_context *ctx, int64_t max_census_photons, uint32
  * the context's current cell opacities and Fleck factors, and written back
  * in place (end states); the CENSUS photons are returned in `census` in
  * their input order with life_dx = c*next_dt; rank_abs_E / rank_track_E
- * (n_cells each) are overwritten with this call's tallies. */
+ * (n_cells each) are overwritten with this call's tallies.  In history mode,
+ * when every photon array is page-locked host memory mapped into the device
+ * (cudaMallocHost, cudaHostAlloc, cudaHostRegister with mapping), the kernels
+ * transport the photons in place there, reading each state at pickup and
+ * writing its end state back over the host link, with no bulk copies
+ * (BGS_OPT_ZERO_COPY turns this off); the results are the same bits. */
 BGS_API int bgs_replicated_transport(bgs_context *ctx, uint64_t n, const bgs_photons_host *photons,
                              double next_dt, uint32_t algorithm, double *rank_abs_E,
                              double *rank_track_E, const bgs_photons_host *census,
@@ -336,9 +341,14 @@ enum {
   BGS_OPT_TRANSPORT_BLOCKS = 3,     /* persistent-grid blocks for the history kernel (0: occupancy);
                                        histories per thread = histories / (blocks * threads) */
   BGS_OPT_TRANSPORT_THREADS = 4,    /* block size of the history kernel: 64, 128 (default) or 256 */
-  BGS_OPT_PIPELINE_MIN_PHOTONS = 5  /* bgs_replicated_transport in history mode overlaps its copies
+  BGS_OPT_PIPELINE_MIN_PHOTONS = 5, /* bgs_replicated_transport in history mode overlaps its copies
                                        with chunked transport from this many photons (default 2^20;
                                        0 never) */
+  BGS_OPT_ZERO_COPY = 6             /* 1 (default): when every photon array given to
+                                       bgs_replicated_transport in history mode is page-locked host
+                                       memory mapped into the device (cudaMallocHost, cudaHostAlloc,
+                                       cudaHostRegister with mapping), the kernels transport the
+                                       photons in place there with no bulk copies; 0: always copy */
 };
 BGS_API int bgs_set_option(bgs_context *ctx, int option, double value);
 

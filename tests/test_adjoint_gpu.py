@@ -88,21 +88,13 @@ def _row_deck(sig, photons, seed):
                 regions=[Region(i + 1, 0.1, 1.0, float(s), 0.0, 0.0, 0.0, 0.1, 0.1) for i, s in enumerate(sig)])
 
 
-def test_gradient_agrees_with_crn_finite_differences(gpu_lib):
-    """Four optically thick cells (sigma_a 20/cm, 0.25 cm), emission only:
-    every cell's gradient is resolved.  Per seed, the adjoint and the CRN
-    central difference (h = 1e-4 relative, counts frozen) use the same
-    photons; over 8 seeds the means must agree within 2% (the estimator does
-    not differentiate the E/E0 < 0.01 cutoff, worth a few tenths of a
-    percent here) plus three standard errors of the paired difference."""
+def _fd_pairs(sig, w, photons, seeds, h=1e-4):
+    """Per seed, the adjoint gradient and the common-random-number central
+    difference (h relative, photon counts frozen) on the same photons."""
     from branson_gb300.adjoint import AdjointStep
-
-    sig = np.array([20.0, 12.0, 30.0, 20.0])
-    w = np.array([0.3, 0.9, 0.1, 0.7])
-    h = 1e-4
     adj, fd = [], []
-    for seed in range(1, 9):
-        with AdjointStep(_row_deck(sig, 200000, seed)) as st:
+    for seed in seeds:
+        with AdjointStep(_row_deck(sig, photons, seed)) as st:
             _, tape = st.forward(sigma_a=sig)
             counts = tape.counts()
             adj.append(st.backward(tape, w))
@@ -116,13 +108,30 @@ def test_gradient_agrees_with_crn_finite_differences(gpu_lib):
                 row.append(np.dot(w, ap - am) / (2 * h * sig[j]))
             fd.append(row)
             tape.close()
-    adj, fd = np.array(adj), np.array(fd)
+    return np.array(adj), np.array(fd)
+
+
+@pytest.mark.parametrize("scale,seeds", [(1.0, 8), (0.2, 16)], ids=["thick", "thin"])
+def test_gradient_agrees_with_crn_finite_differences(gpu_lib, scale, seeds):
+    """Four cells in a row, emission only, 1e6 photons per seed: sigma_a
+    (20, 12, 30, 20)/cm times `scale` in 0.25 cm cells.  Over the seeds the
+    mean adjoint gradient and the mean CRN central difference must agree
+    within 1% plus three standard errors of their paired difference, cell by
+    cell.  The thick row (optical depths 3 to 7.5 per cell) carries the one
+    known bias of the estimator, which does not differentiate the
+    E/E0 < 0.01 cutoff (the jump a killed history makes in the tally,
+    tests/test_adjoint_oracle.py): up to ~1% on the thickest cell.  In the
+    thin row no history decays to the cutoff, and the two agree to a few
+    hundredths of a percent."""
+    sig = np.array([20.0, 12.0, 30.0, 20.0]) * scale
+    w = np.array([0.3, 0.9, 0.1, 0.7])
+    adj, fd = _fd_pairs(sig, w, 1_000_000, range(1, seeds + 1))
     d = adj - fd
     se = d.std(axis=0, ddof=1) / np.sqrt(len(d))
     for j in range(len(sig)):
         print(f"cell {j}: adjoint {adj[:, j].mean():.6e} fd {fd[:, j].mean():.6e} "
               f"rel {d[:, j].mean() / abs(fd[:, j].mean()):+.4f} (se {se[j] / abs(fd[:, j].mean()):.4f})")
-        assert abs(d[:, j].mean()) <= 0.02 * abs(fd[:, j].mean()) + 3.0 * se[j], j
+        assert abs(d[:, j].mean()) <= 0.01 * abs(fd[:, j].mean()) + 3.0 * se[j], j
 
 
 def test_autograd_function(gpu_lib):

@@ -119,3 +119,42 @@ def test_pipelined_dropin_equals_whole_bank(gpu_lib, n):
         assert (ce1, ex1) == (ce0, ex0)
     finally:
         gpu.close()
+
+
+@pytest.mark.parametrize("n", [1, 33, 20928])
+def test_mapped_host_dropin_equals_copied(gpu_lib, n):
+    """With every photon array in page-locked, device-mapped host memory, the
+    drop-in transports the photons in place there (the kernels read and
+    write the caller's arrays; no bulk copies).  Its end states, census,
+    tallies and energies equal those of the copying forms bit for bit
+    (one launch on the device bank, and the pipelined form), and the
+    oracle's within the parity tolerances."""
+    import oracle as O
+    from branson_gb300.engine import arrays_to_records, records_to_arrays
+    dk, orc, gpu, photons, nd = _setup()
+    try:
+        outs = []
+        for zero_copy, min_n in ((1, 0), (0, 0), (0, 1)):
+            gpu.set_option("zero_copy", zero_copy)
+            gpu.set_option("pipeline_min_photons", min_n)
+            ph = records_to_arrays(photons[:n], pinned=True)
+            abs_g, trk_g, census_g, ce_g, ex_g = gpu.replicated_transport(ph, nd)
+            outs.append((arrays_to_records(ph, O.PHOTON_DTYPE), abs_g.copy(), trk_g.copy(),
+                         arrays_to_records(census_g, O.PHOTON_DTYPE), ce_g, ex_g))
+        e0, a0, t0, c0, ce0, ex0 = outs[0]
+        for e1, a1, t1, c1, ce1, ex1 in outs[1:]:
+            for f in e0.dtype.names:
+                np.testing.assert_array_equal(e1[f], e0[f], err_msg=f"end {f}")
+                np.testing.assert_array_equal(c1[f], c0[f], err_msg=f"census {f}")
+            np.testing.assert_array_equal(a1, a0)
+            np.testing.assert_array_equal(t1, t0)
+            assert (ce1, ex1) == (ce0, ex0)
+        mine = photons[:n].copy()
+        abs_o, trk_o, census_o, ce_o, ex_o, _, _ = orc.transport(mine, nd)
+        ext = max(1.0, 299.792458 * dk.dt_start)
+        compare_photons(e0, mine, ext, "mapped end states")
+        compare_photons(c0, census_o, ext, "mapped census")
+        close(a0, abs_o, CELL_RTOL, 0.0, "mapped abs_E")
+        close(t0, trk_o, CELL_RTOL, 0.0, "mapped track_E")
+    finally:
+        gpu.close()
