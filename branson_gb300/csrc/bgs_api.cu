@@ -427,6 +427,10 @@ int bgs_set_mesh(bgs_context *ctx, const bgs_mesh_desc *md) {
   m.T_source = md->T_source;
   m.inv_ngx = div_multiplier(m.ngx);
   m.inv_ngxy = div_multiplier((uint64_t)m.ngx * m.ngy);
+  bool no_scatter = true;  // op_s of every cell is its region's opacS (index 5 of the row)
+  for (uint32_t r = 0; r < md->n_regions; ++r)
+    if (md->regions[8 * (size_t)r + 5] != 0.0) no_scatter = false;
+  m.gray = (md->n_groups == 1 && no_scatter) ? 1u : 0u;
   launch_init_cells(m, c, ctx->stream);
   BGS_LAUNCHED(ctx, 1);
   BGS_CUDA(ctx, cudaMemsetAsync(ctx->d_diag, 0, sizeof(DeviceDiag), ctx->stream));
@@ -463,6 +467,9 @@ int bgs_set_cell_field(bgs_context *ctx, int field, const double *host_in) {
                                 ctx->stream));
   BGS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   if (field != BGS_FIELD_T_E) ctx->xs_dirty = true;
+  if (field == BGS_FIELD_OP_S)  // physical scattering anywhere: the general transport build until the next mesh
+    for (uint32_t g = 0; g < ctx->mesh.n_cells && ctx->mesh.gray; ++g)
+      if (host_in[g] != 0.0) ctx->mesh.gray = 0;
   return BGS_OK;
 }
 

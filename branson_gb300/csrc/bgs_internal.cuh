@@ -89,6 +89,10 @@ struct MeshDev {
   const double *regions;  // n_regions x 8
   int bc[6];
   double T_source;
+  // 1: one group and no physical scattering in any cell (every op_s zero),
+  // so a scatter's effective-scatter test and group resample only advance
+  // the RNG counter; the history kernel then runs a build without them
+  uint32_t gray;
 };
 
 // the multiplier of MeshDev::inv_ngx / inv_ngxy for divisor d >= 1

@@ -373,8 +373,10 @@ __device__ __forceinline__ int segment_advance(const MeshDev &m, const double *E
 
 // Effective scatter (history_based_transport.h:96-99): isotropic new
 // direction (get_uniform_angle, sampling_functions.h:57-70) and, unless
-// physical scattering wins, a resampled group.
-template <bool kFaces = false>
+// physical scattering wins, a resampled group.  kGray: one group and no
+// physical scattering anywhere (MeshDev::gray), where both of those draws
+// only advance the counter (below), so they are left out of the build.
+template <bool kFaces = false, bool kGray = false>
 __device__ __forceinline__ void scatter_update(const MeshDev &m, const CellsDev &c, const CellXS &xs,
                                                Lane &L) {
   const double mu = mu_from_m53(L.rng.next_m53());
@@ -386,6 +388,11 @@ __device__ __forceinline__ void scatter_update(const MeshDev &m, const CellsDev 
   L.dy = sin_theta * sp;
   L.dz = mu;
   load_faces<kFaces>(m, L);
+  if constexpr (kGray) {  // the two draws below, both skipped, and group 0
+    L.rng.ctr += 2;
+    L.group = 0;
+    return;
+  }
   // effective-scatter test and group resample (history_based_transport.h:97-98):
   // with sigma_s = 0 the test u > 0 always passes, and with one group the
   // walk always ends in group 0, so those draws only advance the counter

@@ -48,7 +48,7 @@ __device__ __forceinline__ void add_segments(uint32_t &total, uint32_t segs, Dev
   }
 }
 
-template <bool kResume, int kThreads>
+template <bool kResume, int kThreads, bool kGray = false>
 __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
     k_transport_history(MeshDev m, CellsDev c, Bank b, DeviceDiag *d, unsigned long long seed_hi,
                         EventState es, ItemRange rg) {
@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
       uint32_t surface_cross;
       const int ev = segment_advance(m, b.E0, xs, L, surface_cross, flags);
       if (ev == SEG_SCATTER) {
-        scatter_update(m, c, xs, L);
+        scatter_update<false, kGray>(m, c, xs, L);
       } else {
         int bc = ELEMENT;
         if (ev == SEG_BOUNDARY) bc = face_bc(m, L, surface_cross);
@@ -290,6 +290,19 @@ template <bool kResume>
 void launch_history_kernel(const MeshDev &m, const CellsDev &c, const Bank &b, DeviceDiag *d,
                            unsigned long long seed_hi, const EventState &es, const ItemRange &rg,
                            const TransportLaunch &shape, cudaStream_t s) {
+  if (!kResume && m.gray) {  // one group, no physical scattering: the lean build, same results
+    switch (shape.threads) {
+      case 64:
+        k_transport_history<false, 64, true><<<shape.blocks, 64, 0, s>>>(m, c, b, d, seed_hi, es, rg);
+        return;
+      case 256:
+        k_transport_history<false, 256, true><<<shape.blocks, 256, 0, s>>>(m, c, b, d, seed_hi, es, rg);
+        return;
+      default:
+        k_transport_history<false, 128, true><<<shape.blocks, 128, 0, s>>>(m, c, b, d, seed_hi, es, rg);
+        return;
+    }
+  }
   switch (shape.threads) {
     case 64:
       k_transport_history<kResume, 64><<<shape.blocks, 64, 0, s>>>(m, c, b, d, seed_hi, es, rg);
