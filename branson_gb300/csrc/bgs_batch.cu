@@ -89,6 +89,7 @@ __device__ __forceinline__ void flush_ring_batched(const ProblemView *__restrict
   if (f) atomicOr(&probs[q].d->flags, f);
 }
 
+template <bool kGray>
 __global__ void __launch_bounds__(kTransportThreads, BGS_BATCH_MIN_BLOCKS)
     k_transport_batched(const ProblemView *__restrict__ probs, uint32_t n_probs,
                         const unsigned long long *__restrict__ item_off, unsigned long long *work_counter) {
@@ -160,7 +161,7 @@ __global__ void __launch_bounds__(kTransportThreads, BGS_BATCH_MIN_BLOCKS)
       uint32_t surface_cross;
       const int ev = segment_advance<kBatchFaces>(probs[p].m, probs[p].from.E0, xs, L, surface_cross, flags);
       if (ev == SEG_SCATTER) {
-        scatter_update<kBatchFaces>(probs[p].m, probs[p].c, xs, L);
+        scatter_update<kBatchFaces, kGray>(probs[p].m, probs[p].c, xs, L);
       } else {
         const MeshDev &m = probs[p].m;
         int bc = ELEMENT;
@@ -216,7 +217,7 @@ __global__ void __launch_bounds__(kTransportThreads, BGS_BATCH_MIN_BLOCKS)
 
 TransportLaunch batch_launch_shape(int n_sm) {
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_transport_batched, kTransportThreads, 0) !=
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_transport_batched<false>, kTransportThreads, 0) !=
           cudaSuccess ||
       per_sm < 1)
     per_sm = 1;
@@ -228,9 +229,15 @@ void launch_batch_items(const ProblemView *probs, uint32_t n, unsigned long long
   k_batch_items<<<1, kItemThreads, 0, s>>>(probs, n, item_off, work_counter);
 }
 
+// gray: every problem has one group and no physical scattering (MeshDev::gray),
+// so the lean build, with the same results, runs
 void launch_transport_batched(const ProblemView *probs, uint32_t n, const unsigned long long *item_off,
-                              unsigned long long *work_counter, const TransportLaunch &shape, cudaStream_t s) {
-  k_transport_batched<<<shape.blocks, shape.threads, 0, s>>>(probs, n, item_off, work_counter);
+                              unsigned long long *work_counter, const TransportLaunch &shape, bool gray,
+                              cudaStream_t s) {
+  if (gray)
+    k_transport_batched<true><<<shape.blocks, shape.threads, 0, s>>>(probs, n, item_off, work_counter);
+  else
+    k_transport_batched<false><<<shape.blocks, shape.threads, 0, s>>>(probs, n, item_off, work_counter);
 }
 
 }  // namespace bgs

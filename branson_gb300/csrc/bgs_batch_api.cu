@@ -31,6 +31,7 @@ struct bgs_batch {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   bool step_in_flight = false;
+  bool gray = false;                // every problem gray (MeshDev::gray): the batched launch's lean build
   float last_transport_ms = 0.0f;
   unsigned long long launches = 0;
   std::string err;
@@ -98,7 +99,7 @@ int issue_step(bgs_batch *b) {
   launch_batch_source(b->d_views, b->grid, s);
   launch_batch_bounds(b->d_views, b->grid, s);
   launch_batch_items(b->d_views, n, b->d_item_off, b->d_work, s);
-  launch_transport_batched(b->d_views, n, b->d_item_off, b->d_work, b->shape, s);
+  launch_transport_batched(b->d_views, n, b->d_item_off, b->d_work, b->shape, b->gray, s);
   launch_batch_census_scan(b->d_views, b->grid, s);
   launch_batch_census(b->d_views, b->grid, s);
   launch_batch_finish(b->d_views, b->grid, s);
@@ -228,6 +229,15 @@ int bgs_batch_step(bgs_batch *b, const bgs_step_params *params, bgs_transport_di
     BGS_BCUDA(b, cudaEventRecord(b->order, c->stream));
     BGS_BCUDA(b, cudaStreamWaitEvent(b->stream, b->order, 0));
   }
+  bool gray = true;
+  for (const bgs_context *c : b->ctx) gray = gray && c->mesh.gray;
+  if (gray != b->gray && b->exec) {  // the recorded launch is the other build: record the step again
+    cudaGraphExecDestroy(b->exec);
+    cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+  }
+  b->gray = gray;
   int rc;
   if (b->use_graph) {
     if (!b->exec) {  // record once: every step relaunches the same graph

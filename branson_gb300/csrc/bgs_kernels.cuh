@@ -198,7 +198,8 @@ void launch_batch_bounds(const ProblemView *v, const BatchGrid &g, cudaStream_t 
 void launch_batch_items(const ProblemView *v, uint32_t n, unsigned long long *item_off,
                         unsigned long long *work_counter, cudaStream_t s);
 void launch_transport_batched(const ProblemView *v, uint32_t n, const unsigned long long *item_off,
-                              unsigned long long *work_counter, const TransportLaunch &shape, cudaStream_t s);
+                              unsigned long long *work_counter, const TransportLaunch &shape, bool gray,
+                              cudaStream_t s);
 void launch_batch_census_scan(const ProblemView *v, const BatchGrid &g, cudaStream_t s);
 void launch_batch_census(const ProblemView *v, const BatchGrid &g, cudaStream_t s);
 void launch_batch_finish(const ProblemView *v, const BatchGrid &g, cudaStream_t s);
