@@ -98,6 +98,7 @@ __global__ void __launch_bounds__(kTransportThreads, BGS_BATCH_MIN_BLOCKS)
   const unsigned lanemask_lt = (1u << lane) - 1u;
   if (threadIdx.x == 0) atomicMin(&work_counter[1], global_ns());
   uint32_t flags = 0;
+  uint32_t seg_acc = 0, seg_p = 0;  // segments of ended histories not yet counted, and their problem
   Lane L;
   uint32_t p = 0;
   const CellXS *xs_p = nullptr;
@@ -187,10 +188,22 @@ __global__ void __launch_bounds__(kTransportThreads, BGS_BATCH_MIN_BLOCKS)
     }
     ring_push(ring, tail, tail, flush, ((unsigned long long)p << 32) | fcell, fa, ft);
     if (ended) {
-      const ProblemView &P = probs[p];
-      atomicAdd(&P.d->n_segments, (unsigned long long)L.segs);
+      // a lane's segments are summed while its histories stay in one problem
+      // and added to that problem's count when they move on (consecutive work
+      // items mostly share a problem): one global atomic per history on the
+      // problem's counter serialised the launch on short histories
+      if (seg_acc && seg_p != p) {
+        atomicAdd(&probs[seg_p].d->n_segments, (unsigned long long)seg_acc);
+        seg_acc = 0;
+      }
+      seg_p = p;
+      seg_acc += L.segs;  // a history adds at most 1e8: flushed below 2^31
+      if (seg_acc >= (1u << 31)) {
+        atomicAdd(&probs[p].d->n_segments, (unsigned long long)seg_acc);
+        seg_acc = 0;
+      }
       if (flags) {
-        atomicOr(&P.d->flags, flags);
+        atomicOr(&probs[p].d->flags, flags);
         flags = 0;
       }
       active = false;
@@ -211,6 +224,7 @@ __global__ void __launch_bounds__(kTransportThreads, BGS_BATCH_MIN_BLOCKS)
     flush_ring_batched(probs, take, key, a, t);
     head += k;
   }
+  if (seg_acc) atomicAdd(&probs[seg_p].d->n_segments, (unsigned long long)seg_acc);
   __syncthreads();
   if (threadIdx.x == 0) atomicMax(&work_counter[2], global_ns());
 }
