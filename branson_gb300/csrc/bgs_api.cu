@@ -290,6 +290,7 @@ int bgs_create(bgs_context **out, int device, uint64_t photon_capacity, void *st
                uint64_t n_user_photons) {
   if (!out) return BGS_ERR_INVALID;
   *out = nullptr;
+  if (photon_capacity >= (1ULL << 32)) return BGS_ERR_INVALID;  // bank indices are 32-bit on the device
   int n_dev = 0;
   if (cudaGetDeviceCount(&n_dev) != cudaSuccess || n_dev <= device || device < 0)
     return BGS_ERR_NO_DEVICE;

@@ -84,6 +84,17 @@ BGS_HD uint64_t mulhi(uint64_t a, uint64_t b) {
 #endif
 }
 
+// mulhi(y, b) for b < 2^32 from the high word of y alone: floor(y_hi b / 2^32)
+// is mulhi(y, b) or one below it (one 32 x 32 -> 64-bit product)
+BGS_HD uint64_t mulhi_b32(uint64_t y, uint64_t b) {
+  return ((y >> 32) * (uint64_t)(uint32_t)b) >> 32;
+}
+
+// the high 64 bits of a * b from the high words alone: below mulhi(a, b) by
+// less than 2^33, for the innermost series terms, whose error is scaled down
+// by the higher powers of the small argument
+BGS_HD uint64_t mulhi_hh(uint64_t a, uint64_t b) { return (a >> 32) * (b >> 32); }
+
 BGS_HD int clz64(uint64_t x) {
 #if defined(__CUDA_ARCH__)
   return __clzll((long long)x);
@@ -192,8 +203,8 @@ BGS_HD double neg_log_u53(uint64_t m) {
   // R = r * 2^74 with r = (x - F_j)/F_j < 2^-10
   const uint64_t R = j ? mulhi(f << 11, log_invf(j)) : (f << 11);
   // ln(1+r) = r - r^2 (1/2 - r(1/3 - r(1/4 - r(1/5 - r(1/6 - r/7)))))
-  uint64_t b = 0x2AAAAAAAAAAAAAABULL - (mulhi(R, 0x2492492492492492ULL) >> 10);  // 1/6 - r/7
-  b = 0x3333333333333333ULL - (mulhi(R, b) >> 10);                                // 1/5 - ...
+  uint64_t b = 0x2AAAAAAAAAAAAAABULL - (mulhi_hh(R, 0x2492492492492492ULL) >> 10);  // 1/6 - r/7
+  b = 0x3333333333333333ULL - (mulhi_hh(R, b) >> 10);                                // 1/5 - ...
   b = 0x4000000000000000ULL - (mulhi(R, b) >> 10);                                // 1/4 - ...
   b = 0x5555555555555555ULL - (mulhi(R, b) >> 10);                                // 1/3 - ...
   b = 0x8000000000000000ULL - (mulhi(R, b) >> 10);                                // 1/2 - ...
@@ -239,7 +250,7 @@ BGS_HD double exp_neg(double tau) {
   // s * 2^73 (s < ln2/1024 < 2^-10.5)
   const uint64_t s73 = (uint64_t)(S >> 23);
   // e^-s = 1 - s (1 - s (1/2 - s (1/6 - s (1/24 - s/120))))
-  uint64_t b = 0x0AAAAAAAAAAAAAABULL - (mulhi(s73, 0x0222222222222222ULL) >> 9);  // 1/24 - s/120
+  uint64_t b = 0x0AAAAAAAAAAAAAABULL - (mulhi_hh(s73, 0x0222222222222222ULL) >> 9);  // 1/24 - s/120
   b = 0x2AAAAAAAAAAAAAABULL - (mulhi(s73, b) >> 9);                                // 1/6 - ...
   b = 0x8000000000000000ULL - (mulhi(s73, b) >> 9);                                // 1/2 - ...
   b = (uint64_t)0 - (mulhi(s73, b) >> 9);                                          // 1 - s(...) (mod 2^64)
@@ -327,13 +338,15 @@ BGS_HD SinCos sincos_phi_v(double phi) {
     const uint64_t y = mulhi(th64, th64);                    // theta^2 * 2^64
     uint64_t b = kS[fixtab::kSinTerms - 1];
 #pragma unroll
-    for (int k = fixtab::kSinTerms - 2; k >= 0; --k) b = kS[k] - mulhi(y, b);  // ~1/3! - y(1/5! - ...)
+    for (int k = fixtab::kSinTerms - 2; k >= 0; --k)  // ~1/3! - y(1/5! - ...)
+      b = kS[k] - (kS[k + 1] < (1ULL << 32) ? mulhi_b32(y, b) : mulhi(y, b));
     const uint64_t sb = mulhi(y, b);                          // y * b
     const u128 Ws = sb ? (u128)Tm * ((uint64_t)0 - sb) : ((u128)Tm << 64);
     sv = round_u128_high(Ws, 122 + lz);  // Ws in [2^124, 2^127)
     uint64_t c = kCo[fixtab::kCosTerms - 1];
 #pragma unroll
-    for (int k = fixtab::kCosTerms - 2; k >= 0; --k) c = kCo[k] - mulhi(y, c);  // ~1/2! - y(1/4! - ...)
+    for (int k = fixtab::kCosTerms - 2; k >= 0; --k)  // ~1/2! - y(1/4! - ...)
+      c = kCo[k] - (kCo[k + 1] < (1ULL << 32) ? mulhi_b32(y, c) : mulhi(y, c));
     const uint64_t cb = mulhi(y, c);
     cv = cb ? round_unit_q64((uint64_t)0 - cb) : 1.0;  // cos >= cos(pi/4): 2^64 - cb >= 2^63
   }

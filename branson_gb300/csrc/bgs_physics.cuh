@@ -42,7 +42,7 @@ struct Lane {
   double fx, fy, fz;  // the current cell's face planes ahead along x, y, z (kFaces)
   double thr_abs;   // absorbed energy of the current cell visit
   double thr_dep;   // the remaining energy a cutoff kill deposits (visit_deposit)
-  unsigned long long idx;
+  uint32_t idx;  // bank index (bgs_create keeps banks below 2^32 photons)
   Rng rng;
   uint32_t cell, group, ci, cj, ck, segs;
 };

@@ -135,9 +135,11 @@ enum {
 
 /* ------------------------------------------------------------ lifecycle */
 /* Create a context on `device` with room for `photon_capacity` photons per
- * bank.  `stream` is a cudaStream_t to launch on (NULL: the context creates
- * its own non-blocking stream).  seed and n_user_photons are the deck's
- * <seed> and <photons> (imc_parameters.h:30-40). */
+ * bank (below 2^32: BGS_ERR_INVALID otherwise; two banks of 2^32 photons
+ * would not fit in the device memory anyway).  `stream` is a cudaStream_t to
+ * launch on (NULL: the context creates its own non-blocking stream).  seed
+ * and n_user_photons are the deck's <seed> and <photons>
+ * (imc_parameters.h:30-40). */
 BGS_API int bgs_create(bgs_context **ctx, int device, uint64_t photon_capacity, void *stream,
                uint32_t seed, uint64_t n_user_photons);
 BGS_API int bgs_destroy(bgs_context *ctx);

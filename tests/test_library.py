@@ -45,6 +45,16 @@ def test_no_cpu_fallback_without_gpu():
     assert lib.bgs_status_string(rc) == b"no usable sm_103 device"
 
 
+def test_bank_capacity_limit_is_checked_first():
+    """Bank indices are 32-bit on the device: bgs_create rejects a capacity
+    of 2^32 photons before it looks for a device."""
+    from branson_gb300 import _lib
+    lib = _lib.load()
+    ctx = C.c_void_p()
+    assert lib.bgs_create(C.byref(ctx), 0, 1 << 32, None, 777, 100) == _lib.ERR_INVALID
+    assert not ctx.value
+
+
 def test_engine_fails_loudly_without_gpu():
     import torch
     if torch.cuda.is_available():
