@@ -48,10 +48,23 @@ __device__ __forceinline__ void add_segments(uint32_t &total, uint32_t segs, Dev
   }
 }
 
-template <bool kResume, int kThreads, bool kGray = false>
+// Small meshes (kStagedCellsMax cells or fewer: the hot-loop table of one
+// such mesh is at most 16 KB) run a build that copies the whole per-cell
+// transport table into each block's shared memory at launch and reads every
+// segment's CellXS from there; larger tables stay in global memory behind
+// L1 (a block's lanes roam the whole mesh, so no smaller per-block set of
+// cells exists to stage).
+constexpr uint32_t kStagedCellsMax = 16384 / sizeof(CellXS);
+
+template <bool kResume, int kThreads, bool kGray = false, bool kStaged = false>
 __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
     k_transport_history(MeshDev m, CellsDev c, Bank b, DeviceDiag *d, unsigned long long seed_hi,
                         EventState es, ItemRange rg) {
+  extern __shared__ CellXS staged_xs[];  // kStaged: the mesh's n_cells entries
+  if constexpr (kStaged) {
+    for (uint32_t g = threadIdx.x; g < m.n_cells; g += kThreads) staged_xs[g] = c.xs[g];
+    __syncthreads();
+  }
   const unsigned long long n = kResume ? (unsigned long long)*es.n_active : (rg.queue ? rg.count : d->n_bank);
   unsigned long long *const queue = rg.queue ? rg.queue : &d->work_counter;
   const int sa = d->scale_abs;
@@ -111,7 +124,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
     uint32_t fcell = 0;
     double fa = 0.0, ft = 0.0;
     if (active) {
-      const CellXS xs = c.xs[L.cell];
+      const CellXS xs = kStaged ? staged_xs[L.cell] : c.xs[L.cell];
       uint32_t surface_cross;
       const int ev = segment_advance(m, b.E0, xs, L, surface_cross, flags);
       if (ev == SEG_SCATTER) {
@@ -286,20 +299,37 @@ TransportLaunch transport_launch_shape(int n_sm, int threads) {
   }
 }
 
+// the whole-bank builds: gray or not, the cell table staged in shared
+// memory or not (the same arithmetic, so the same results)
+template <int kThreads, bool kGray>
+void launch_history_whole(const MeshDev &m, const CellsDev &c, const Bank &b, DeviceDiag *d,
+                          unsigned long long seed_hi, const EventState &es, const ItemRange &rg, int blocks,
+                          cudaStream_t s) {
+  if (m.n_cells <= kStagedCellsMax) {
+    k_transport_history<false, kThreads, kGray, true>
+        <<<blocks, kThreads, m.n_cells * sizeof(CellXS), s>>>(m, c, b, d, seed_hi, es, rg);
+  } else {
+    k_transport_history<false, kThreads, kGray><<<blocks, kThreads, 0, s>>>(m, c, b, d, seed_hi, es, rg);
+  }
+}
+
 template <bool kResume>
 void launch_history_kernel(const MeshDev &m, const CellsDev &c, const Bank &b, DeviceDiag *d,
                            unsigned long long seed_hi, const EventState &es, const ItemRange &rg,
                            const TransportLaunch &shape, cudaStream_t s) {
-  if (!kResume && m.gray) {  // one group, no physical scattering: the lean build, same results
+  if (!kResume) {  // gray (one group, no physical scattering): the lean build, same results
     switch (shape.threads) {
       case 64:
-        k_transport_history<false, 64, true><<<shape.blocks, 64, 0, s>>>(m, c, b, d, seed_hi, es, rg);
+        if (m.gray) launch_history_whole<64, true>(m, c, b, d, seed_hi, es, rg, shape.blocks, s);
+        else launch_history_whole<64, false>(m, c, b, d, seed_hi, es, rg, shape.blocks, s);
         return;
       case 256:
-        k_transport_history<false, 256, true><<<shape.blocks, 256, 0, s>>>(m, c, b, d, seed_hi, es, rg);
+        if (m.gray) launch_history_whole<256, true>(m, c, b, d, seed_hi, es, rg, shape.blocks, s);
+        else launch_history_whole<256, false>(m, c, b, d, seed_hi, es, rg, shape.blocks, s);
         return;
       default:
-        k_transport_history<false, 128, true><<<shape.blocks, 128, 0, s>>>(m, c, b, d, seed_hi, es, rg);
+        if (m.gray) launch_history_whole<128, true>(m, c, b, d, seed_hi, es, rg, shape.blocks, s);
+        else launch_history_whole<128, false>(m, c, b, d, seed_hi, es, rg, shape.blocks, s);
         return;
     }
   }
