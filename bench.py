@@ -389,10 +389,10 @@ def run_ours(args, rank, world, local):
     imc.close()
     adjoint = None
     if not args.no_adjoint and rank == 0 and world == 1:
-        adjoint = guarded(adjoint_bench, args, dev)
+        adjoint = guarded(adjoint_bench, args, dev, clocks_of=dev)
     batched = None
     if not args.no_batch and rank == 0 and world == 1:
-        batched = guarded(batch_bench, args, dev)
+        batched = guarded(batch_bench, args, dev, clocks_of=dev)
     decks = None
     if not args.no_decks and rank == 0 and world == 1 and args.workload == "hot_zone":
         decks = guarded(decks_bench, dev)
@@ -469,6 +469,8 @@ def deck_rate(dk, dev, cfg, cpu_steps=None):
     import torch
     from branson_gb300.engine import ReplicatedIMC
     n_steps = int(round((dk.t_stop - dk.t_start) / dk.dt_start))
+    clocks = Clocks(dev)  # sampled over the GPU part only (warm-up context and the timed steps)
+    clocks.start()
     with ReplicatedIMC(copy.deepcopy(dk), device=dev) as w:
         w.step(sync=True)
     stream = torch.cuda.Stream(device=dev)
@@ -487,11 +489,12 @@ def deck_rate(dk, dev, cfg, cpu_steps=None):
         ev1.record(stream)
         torch.cuda.synchronize()
         el = ev0.elapsed_time(ev1) / 1e3
+    clk = clocks.stop()
     threads = os.cpu_count() or 1
     cs = n_steps if cpu_steps is None else cpu_steps
     h, s, sg, wall = cpu_port_rate(dk, threads, steps=cs, warmup=0)
     return dict(cfg, steps=n_steps, histories=int(hist), segments=int(segs), gpu_s=el, transport_kernel_s=kms / 1e3,
-                histories_per_s=hist / el, segments_per_s=segs / el,
+                histories_per_s=hist / el, segments_per_s=segs / el, clocks=clk,
                 cpu={"histories_per_s": h / s, "segments_per_s": sg / s, "cores": threads, "kind": "port",
                      "steps": cs, "histories": int(h), "transport_s": s, "wall_s": wall,
                      "sample": "the same deck and photons per step from step 1, transport time only"},
@@ -630,13 +633,21 @@ def fd_forward(st, sigma_a, counts):
         return st.forward(sigma_a=sigma_a, counts=counts, save=False)[0]
 
 
-def guarded(fn, *a):
+def guarded(fn, *a, clocks_of=None):
     """A bench section whose failure is reported in its own key instead of
-    ending the run before the headline line is printed."""
+    ending the run before the headline line is printed.  With clocks_of (a
+    device index) the section's SM clocks and throttle reasons are sampled
+    while it runs and returned in its "clocks" key."""
+    clk = Clocks(clocks_of) if clocks_of is not None else None
+    if clk:
+        clk.start()
     try:
-        return fn(*a)
+        out = fn(*a)
     except Exception as e:  # reported, not hidden: the section's JSON holds the error
-        return {"error": f"{type(e).__name__}: {e}"}
+        out = {"error": f"{type(e).__name__}: {e}"}
+    if clk:
+        out["clocks"] = clk.stop()
+    return out
 
 
 def adjoint_bench(args, dev, replicas: int = 6):
