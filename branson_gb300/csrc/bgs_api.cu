@@ -398,7 +398,7 @@ int bgs_set_mesh(bgs_context *ctx, const bgs_mesh_desc *md) {
     return rc;
   CellsDev &c = ctx->cells;
   double **dbl[] = {&c.T_e, &c.T_r, &c.T_s, &c.op_a, &c.op_s, &c.f, &c.em_E, &c.ce_E, &c.so_E,
-                    &c.T_r_diag, &c.group_v, &ctx->d_mat_E, &ctx->d_abs, &ctx->d_track};
+                    &c.T_r_diag, &c.group_v, &c.inv_saf, &ctx->d_mat_E, &ctx->d_abs, &ctx->d_track};
   for (double **p : dbl)
     if ((rc = dev_alloc(ctx, L, p, n))) return rc;
   if ((rc = dev_alloc(ctx, L, &c.xs, n)) || (rc = dev_alloc(ctx, L, &c.tally, n)) ||

@@ -48,15 +48,15 @@ constexpr uint32_t kMaxSegmentsPerHistory = 100000000u;
 // those of the upstream loop:
 //   sig_eff  = (1 - f)*sigma_a + sigma_s   (effective scattering opacity)
 //   neg_saf  = -sigma_a * f                (exponent rate, negated)
-//   inv_saf  = 1/(sigma_a * f)            (track-length factor; the tally
-//                                          contribution absorbed/(sigma_a f) is
-//                                          formed as a product, within 1 ulp)
 //   p_scat   = sigma_s / sig_eff           (physical-scatter probability)
 //   inv_se   = RN(1/sig_eff) for the correctly rounded division
 //              -log(u)/sig_eff by one multiply and two fma (div_recip in
 //              bgs_physics.cuh); 0 if sig_eff is 0 or out of that range
-struct __align__(16) CellXS {
-  double sig_eff, neg_saf, inv_saf, p_scat, inv_se;
+// One entry is one 32-byte sector: a segment's table read is one sector.
+// The track-length factor RN(1/(sigma_a f)), read once per cell per step
+// when the tallies are converted, is in its own array (CellsDev::inv_saf).
+struct __align__(32) CellXS {
+  double sig_eff, neg_saf, p_scat, inv_se;
 };
 
 // 128-bit fixed-point tally cell: value = (hi*2^64 + lo) * 2^-scale_abs.
@@ -119,6 +119,8 @@ struct CellsDev {
   double *T_e, *T_r, *T_s, *op_a, *op_s, *f, *em_E, *ce_E, *so_E, *T_r_diag;
   double *group_v;        // op_a * (1/(op_a*N)): one CDF step of sample_emission_group
   CellXS *xs;
+  double *inv_saf;        // RN(1/(op_a f)): the track-length factor (the tally contribution
+                          // absorbed/(sigma_a f) is formed as a product, within 1 ulp)
   TallyCell *tally;
   int8_t *source_face;    // Cell::get_source_face (cell.h:69-76), -1 if none
   uint32_t *n_em, *n_so, *n_ce;          // photons per cell

@@ -88,12 +88,12 @@ __device__ __forceinline__ void set_cell_xs(const CellsDev &c, uint32_t g, doubl
   CellXS x;
   x.sig_eff = (1.0 - f) * op_a + op_s;
   x.neg_saf = -op_a * f;
-  x.inv_saf = 1.0 / (op_a * f);
   // op_s / sigma_eff; a zero op_s over a positive finite sigma_eff is op_s itself
   x.p_scat = (op_s == 0.0 && x.sig_eff > 0.0 && x.sig_eff < 1.7976931348623157e308) ? op_s
                                                                                    : op_s / x.sig_eff;
   x.inv_se = recip_for_div(x.sig_eff);
   c.xs[g] = x;
+  c.inv_saf[g] = 1.0 / (op_a * f);
   // read only by the multigroup resample (sample_group)
   if (n_groups > 1) {
     const double norm_factor = 1.0 / (op_a * (double)n_groups);

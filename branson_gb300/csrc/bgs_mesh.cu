@@ -473,7 +473,7 @@ __device__ __forceinline__ void tally_to_double_body(const MeshDev &m, const Cel
       // a cell that absorbed nothing has none (TallyCell)
       const unsigned long long vlo = t.abs_lo - t.dep_lo;
       const unsigned long long vhi = t.abs_hi - t.dep_hi - (t.abs_lo < t.dep_lo ? 1ULL : 0ULL);
-      track_out[g] = (vlo | vhi) ? from_fixed128(vlo, vhi, d->scale_abs) * c.xs[g].inv_saf : 0.0;
+      track_out[g] = (vlo | vhi) ? from_fixed128(vlo, vhi, d->scale_abs) * c.inv_saf[g] : 0.0;
       alo = t.abs_lo;
       ahi = t.abs_hi;
     }

@@ -41,7 +41,8 @@ struct NoAllocLayout {
   static constexpr size_t tally = 0;
   static constexpr size_t xs = tally + sizeof(TallyCell) * kNoAllocMaxCells;
   static constexpr size_t group_v = xs + sizeof(CellXS) * kNoAllocMaxCells;
-  static constexpr size_t diag = (group_v + sizeof(double) * kNoAllocMaxCells + 255) & ~size_t(255);
+  static constexpr size_t inv_saf = group_v + sizeof(double) * kNoAllocMaxCells;
+  static constexpr size_t diag = (inv_saf + sizeof(double) * kNoAllocMaxCells + 255) & ~size_t(255);
   static constexpr size_t maxbits = (diag + sizeof(DeviceDiag) + 255) & ~size_t(255);
   static constexpr size_t bytes = maxbits + 2 * sizeof(unsigned long long);
 };
@@ -120,6 +121,7 @@ extern "C" BGS_API int bgs_transport_device_noalloc(
   c.tally = reinterpret_cast<TallyCell *>(base + NoAllocLayout::tally);
   c.xs = reinterpret_cast<CellXS *>(base + NoAllocLayout::xs);
   c.group_v = reinterpret_cast<double *>(base + NoAllocLayout::group_v);
+  c.inv_saf = reinterpret_cast<double *>(base + NoAllocLayout::inv_saf);
   DeviceDiag *d = reinterpret_cast<DeviceDiag *>(base + NoAllocLayout::diag);
   unsigned long long *maxbits = reinterpret_cast<unsigned long long *>(base + NoAllocLayout::maxbits);
   Bank b{p.pos_x, p.pos_y, p.pos_z, p.dir_x, p.dir_y, p.dir_z, p.E, p.E0, p.life_dx, p.cell, p.group,
