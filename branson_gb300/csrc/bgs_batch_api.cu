@@ -21,6 +21,8 @@ struct bgs_batch {
   std::vector<void *> allocs;
   ProblemView *d_views = nullptr;
   ProblemView *h_views = nullptr;   // pinned staging of the view table
+  DeviceDiag *d_diags = nullptr;    // every problem's diagnostics after a step, gathered
+  DeviceDiag *h_diags = nullptr;    // pinned copy of d_diags, written by the step itself
   BatchGrid grid{};
   unsigned long long *d_item_off = nullptr;
   unsigned long long *d_work = nullptr;  // queue head, launch start and end stamps (ns)
@@ -41,8 +43,8 @@ namespace {
 
 // launches of one batched step: begin 1, energies and counts 12, sourcing 3,
 // scales 2, items + transport 2, census offsets 3, census 2, tallies and
-// temperatures 4
-constexpr unsigned long long kLaunchesPerStep = 29;
+// temperatures 4, diagnostics gather 1
+constexpr unsigned long long kLaunchesPerStep = 30;
 
 uint32_t blocks_for(unsigned long long items, uint32_t per_block, uint32_t cap) {
   const unsigned long long b = (items + per_block - 1) / per_block;
@@ -103,6 +105,10 @@ int issue_step(bgs_batch *b) {
   launch_batch_census_scan(b->d_views, b->grid, s);
   launch_batch_census(b->d_views, b->grid, s);
   launch_batch_finish(b->d_views, b->grid, s);
+  // the diagnostics of all problems reach the host in one copy (n small
+  // synchronous copies after the step cost more than the whole census phase)
+  launch_batch_diag_gather(b->d_views, n, b->d_diags, s);
+  BGS_BCUDA(b, cudaMemcpyAsync(b->h_diags, b->d_diags, n * sizeof(DeviceDiag), cudaMemcpyDeviceToHost, s));
   BGS_BCUDA(b, cudaGetLastError());
   b->launches += kLaunchesPerStep;
   return BGS_OK;
@@ -153,12 +159,19 @@ int bgs_batch_create(bgs_batch **out, uint32_t n, bgs_context *const *contexts) 
       cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&b->order, cudaEventDisableTiming) != cudaSuccess ||
-      cudaMallocHost(&b->h_views, n * sizeof(ProblemView)) != cudaSuccess)
+      cudaMallocHost(&b->h_views, n * sizeof(ProblemView)) != cudaSuccess ||
+      cudaMallocHost(&b->h_diags, n * sizeof(DeviceDiag)) != cudaSuccess)
     rc = BGS_ERR_CUDA;
   void *q = nullptr;
   if (!rc && cudaMalloc(&q, n * sizeof(ProblemView)) == cudaSuccess) {
     b->allocs.push_back(q);
     b->d_views = static_cast<ProblemView *>(q);
+  } else {
+    rc = BGS_ERR_CUDA;
+  }
+  if (!rc && cudaMalloc(&q, n * sizeof(DeviceDiag)) == cudaSuccess) {
+    b->allocs.push_back(q);
+    b->d_diags = static_cast<DeviceDiag *>(q);
   } else {
     rc = BGS_ERR_CUDA;
   }
@@ -199,6 +212,7 @@ int bgs_batch_destroy(bgs_batch *b) {
   if (b->graph) cudaGraphDestroy(b->graph);
   for (void *p : b->allocs) cudaFree(p);
   if (b->h_views) cudaFreeHost(b->h_views);
+  if (b->h_diags) cudaFreeHost(b->h_diags);
   if (b->done) cudaEventDestroy(b->done);
   if (b->order) cudaEventDestroy(b->order);
   if (b->stream) cudaStreamDestroy(b->stream);
@@ -273,7 +287,7 @@ int bgs_batch_step(bgs_batch *b, const bgs_step_params *params, bgs_transport_di
     b->step_in_flight = false;
     for (uint32_t i = 0; i < n; ++i) {
       bgs_context *c = b->ctx[i];
-      BGS_BCUDA(b, cudaMemcpy(c->h_diag, c->d_diag, sizeof(DeviceDiag), cudaMemcpyDeviceToHost));
+      *c->h_diag = b->h_diags[i];  // copied by the step (issue_step)
       const DeviceDiag &d = *c->h_diag;
       bgs_transport_diag &o = out[i];
       o.n_transported = d.n_bank;

@@ -203,6 +203,8 @@ void launch_transport_batched(const ProblemView *v, uint32_t n, const unsigned l
 void launch_batch_census_scan(const ProblemView *v, const BatchGrid &g, cudaStream_t s);
 void launch_batch_census(const ProblemView *v, const BatchGrid &g, cudaStream_t s);
 void launch_batch_finish(const ProblemView *v, const BatchGrid &g, cudaStream_t s);
+// every problem's DeviceDiag gathered into out[0..n) (one copy to the host instead of n)
+void launch_batch_diag_gather(const ProblemView *v, uint32_t n, DeviceDiag *out, cudaStream_t s);
 
 // adjoint replay of a saved photon bank (bgs_adjoint.cu)
 TransportLaunch adjoint_launch_shape(int n_sm);

@@ -755,4 +755,15 @@ void launch_batch_finish(const ProblemView *v, const BatchGrid &g, cudaStream_t 
   k_b_finish_temperature<<<dim3(1, g.n), 32, 0, s>>>(v);
 }
 
+static_assert(sizeof(DeviceDiag) % sizeof(unsigned long long) == 0, "DeviceDiag is copied in 8-byte words");
+__global__ void k_b_diag_gather(const ProblemView *v, DeviceDiag *out) {
+  const unsigned long long *from = reinterpret_cast<const unsigned long long *>(v[blockIdx.x].d);
+  unsigned long long *to = reinterpret_cast<unsigned long long *>(out + blockIdx.x);
+  for (uint32_t k = threadIdx.x; k < sizeof(DeviceDiag) / sizeof(unsigned long long); k += blockDim.x) to[k] = from[k];
+}
+
+void launch_batch_diag_gather(const ProblemView *v, uint32_t n, DeviceDiag *out, cudaStream_t s) {
+  k_b_diag_gather<<<n, 32, 0, s>>>(v, out);
+}
+
 }  // namespace bgs
