@@ -336,6 +336,9 @@ BGS_HD SinCos sincos_phi_v(double phi) {
     const uint64_t Tm = mulhi(Xn, fixtab::kPiOver2_q62);     // theta = Tm * 2^(-58-lz)
     const uint64_t th64 = lz >= 6 ? (lz - 6 >= 64 ? 0 : Tm >> (lz - 6)) : Tm << (6 - lz);  // theta * 2^64
     const uint64_t y = mulhi(th64, th64);                    // theta^2 * 2^64
+    // the running term never exceeds the coefficient it started from, so
+    // where that coefficient is below 2^32 one 32 x 32-bit product serves
+    // (the two innermost steps of each series)
     uint64_t b = kS[fixtab::kSinTerms - 1];
 #pragma unroll
     for (int k = fixtab::kSinTerms - 2; k >= 0; --k)  // ~1/3! - y(1/5! - ...)
