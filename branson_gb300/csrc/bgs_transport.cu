@@ -48,21 +48,33 @@ __device__ __forceinline__ void add_segments(uint32_t &total, uint32_t segs, Dev
   }
 }
 
-// Small meshes (kStagedCellsMax cells or fewer: the hot-loop table of one
-// such mesh is at most 16 KB) run a build that copies the whole per-cell
-// transport table into each block's shared memory at launch and reads every
-// segment's CellXS from there; larger tables stay in global memory behind
-// L1 (a block's lanes roam the whole mesh, so no smaller per-block set of
-// cells exists to stage).
-constexpr uint32_t kStagedCellsMax = 16384 / sizeof(CellXS);
+// Small meshes (kStagedCellsMax cells or fewer: 16 KB of per-cell data)
+// run a build that keeps each block's cells in its shared memory: the whole
+// per-cell transport table, copied in at launch and read by every segment,
+// and the block's own 128-bit tallies, which its visit flushes add to with
+// shared-memory atomics and which go to the global tallies once, when the
+// block ends (few cells take every flush of the launch: global atomics on
+// them queue in L2).  Integer sums do not depend on the order of the adds,
+// so the tallies are the same bits.  Larger meshes keep both in global
+// memory behind L1 (a block's lanes roam the whole mesh, so no smaller
+// per-block set of cells exists to stage).
+constexpr uint32_t kStagedCellsMax = 16384 / (sizeof(CellXS) + sizeof(TallyCell));
+constexpr size_t staged_bytes(uint32_t n_cells) { return (size_t)n_cells * (sizeof(CellXS) + sizeof(TallyCell)); }
 
 template <bool kResume, int kThreads, bool kGray = false, bool kStaged = false>
 __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
     k_transport_history(MeshDev m, CellsDev c, Bank b, DeviceDiag *d, unsigned long long seed_hi,
                         EventState es, ItemRange rg) {
-  extern __shared__ CellXS staged_xs[];  // kStaged: the mesh's n_cells entries
+  // kStaged: the mesh's n_cells CellXS entries, then the block's n_cells tallies
+  extern __shared__ __align__(32) unsigned char staged[];
+  CellXS *const staged_xs = reinterpret_cast<CellXS *>(staged);
+  TallyCell *const staged_tally = reinterpret_cast<TallyCell *>(staged + (size_t)m.n_cells * sizeof(CellXS));
+  TallyCell *const tally = kStaged ? staged_tally : c.tally;
   if constexpr (kStaged) {
-    for (uint32_t g = threadIdx.x; g < m.n_cells; g += kThreads) staged_xs[g] = c.xs[g];
+    for (uint32_t g = threadIdx.x; g < m.n_cells; g += kThreads) {
+      staged_xs[g] = c.xs[g];
+      staged_tally[g] = TallyCell{0ULL, 0ULL, 0ULL, 0ULL};
+    }
     __syncthreads();
   }
   const unsigned long long n = kResume ? (unsigned long long)*es.n_active : (rg.queue ? rg.count : d->n_bank);
@@ -158,7 +170,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
       unsigned long long key;
       double a, t;
       ring_take(ring, head, 32u, key, a, t);
-      flush_tally_warp(c.tally, true, (uint32_t)key, (uint32_t)key, a, t, flags, sa);
+      flush_tally_warp(tally, true, (uint32_t)key, (uint32_t)key, a, t, flags, sa);
       head += 32u;
     }
   }
@@ -167,8 +179,17 @@ __global__ void __launch_bounds__(kThreads, min_blocks_for<kThreads>())
     unsigned long long key;
     double a, t;
     const bool take = ring_take(ring, head, k, key, a, t);
-    flush_tally_warp(c.tally, take, (uint32_t)key, (uint32_t)key, a, t, flags, sa);
+    flush_tally_warp(tally, take, (uint32_t)key, (uint32_t)key, a, t, flags, sa);
     head += k;
+  }
+  if constexpr (kStaged) {  // the block's tallies into the global ones
+    __syncthreads();
+    for (uint32_t g = threadIdx.x; g < m.n_cells; g += kThreads) {
+      const TallyCell s = staged_tally[g];
+      TallyCell *tc = &c.tally[g];
+      if (s.abs_lo | s.abs_hi) atomic_add128(&tc->abs_lo, &tc->abs_hi, s.abs_lo, s.abs_hi);
+      if (s.dep_lo | s.dep_hi) atomic_add128(&tc->dep_lo, &tc->dep_hi, s.dep_lo, s.dep_hi);
+    }
   }
 
   // ---- per-warp totals
@@ -307,7 +328,7 @@ void launch_history_whole(const MeshDev &m, const CellsDev &c, const Bank &b, De
                           cudaStream_t s) {
   if (m.n_cells <= kStagedCellsMax) {
     k_transport_history<false, kThreads, kGray, true>
-        <<<blocks, kThreads, m.n_cells * sizeof(CellXS), s>>>(m, c, b, d, seed_hi, es, rg);
+        <<<blocks, kThreads, staged_bytes(m.n_cells), s>>>(m, c, b, d, seed_hi, es, rg);
   } else {
     k_transport_history<false, kThreads, kGray><<<blocks, kThreads, 0, s>>>(m, c, b, d, seed_hi, es, rg);
   }
