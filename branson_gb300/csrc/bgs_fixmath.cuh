@@ -242,11 +242,11 @@ BGS_HD double exp_neg(double tau) {
   uint64_t N = mulhi(A, fixtab::kInvLn2_1024_q32);
   const u128 L = ((u128)fixtab::kLn2_1024_96_hi << 64) | fixtab::kLn2_1024_96_lo;
   u128 NL = L * N;
-#pragma unroll 1
-  for (int it = 0; it < 4 && NL > T; ++it) { --N; NL -= L; }
+  // N is then the floor or one off it either way: one predicated step each
+  // way (no loop; the upward one runs for about a tenth of the arguments)
+  if (NL > T) { --N; NL -= L; }
   u128 S = T - NL;
-#pragma unroll 1
-  for (int it = 0; it < 4 && S >= L; ++it) { ++N; S -= L; }
+  if (S >= L) { ++N; S -= L; }
   // s * 2^73 (s < ln2/1024 < 2^-10.5)
   const uint64_t s73 = (uint64_t)(S >> 23);
   // e^-s = 1 - s (1 - s (1/2 - s (1/6 - s (1/24 - s/120))))

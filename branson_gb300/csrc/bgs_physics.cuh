@@ -38,7 +38,7 @@ __device__ __forceinline__ double div_recip(double a, double b, double y) {
 // (kFaces); the others read them from the mesh planes per segment.
 struct Lane {
   double px, py, pz, dx, dy, dz, E, life;
-  double kill_thr;  // RN(0.01 * E0): the cutoff test runs against it in integer ulps
+  long long kill_key;  // f64_key(RN(0.01 * E0)): the cutoff test runs against it in integer ulps
   double fx, fy, fz;  // the current cell's face planes ahead along x, y, z (kFaces)
   double thr_abs;   // absorbed energy of the current cell visit
   double thr_dep;   // the remaining energy a cutoff kill deposits (visit_deposit)
@@ -59,8 +59,6 @@ __device__ __forceinline__ void load_faces(const MeshDev &m, Lane &L) {
   }
 }
 
-// a history's birth weight: the cutoff threshold RN(0.01 E0)
-__device__ __forceinline__ void set_birth(Lane &L, double E0) { L.kill_thr = kCutoff * E0; }
 
 // Warp-aggregated tally flush of cell visits (a: the visit's absorbed
 // energy, t: the part of it a cutoff kill deposited; TallyCell): every lane
@@ -190,6 +188,9 @@ __device__ __forceinline__ long long f64_key(double x) {
   return b >= 0 ? b : (b ^ 0x7FFFFFFFFFFFFFFFLL);
 }
 __device__ __forceinline__ bool f64_positive(double x) { return __double_as_longlong(x) > 0; }
+
+// a history's birth weight: the key of the cutoff threshold RN(0.01 E0)
+__device__ __forceinline__ void set_birth(Lane &L, double E0) { L.kill_key = f64_key(kCutoff * E0); }
 
 // what one segment ends in (the event branches of transport_photon)
 enum SegEvent : int { SEG_KILLED = 0, SEG_SCATTER = 1, SEG_BOUNDARY = 2, SEG_CENSUS = 3 };
@@ -357,7 +358,7 @@ __device__ __forceinline__ int segment_advance(const MeshDev &m, const double *E
   // below_cutoff: E/E0 < 0.01 (photon.h:47-49).  More than four ulps from
   // RN(0.01*E0), E < RN(0.01*E0) decides it the same way as RN(E/E0) < 0.01;
   // closer than that the exact quotient settles it
-  const long long k_e = f64_key(L.E), k_thr = f64_key(L.kill_thr);
+  const long long k_e = f64_key(L.E), k_thr = L.kill_key;
   bool killed = k_e < k_thr;
   if (k_e - k_thr <= 4 && k_thr - k_e <= 4) killed = L.E / E0s[L.idx] < kCutoff;
   if (killed || L.segs >= kMaxSegmentsPerHistory) {
