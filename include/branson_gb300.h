@@ -149,27 +149,46 @@ BGS_API const char *bgs_status_string(int status);
 BGS_API const char *bgs_version(void);
 
 /* ---------------------------------------------------------------- mesh */
+/* The replicated Mesh (mesh.h:50-150, built from the deck by its
+ * constructor at mesh.h:54) uploaded once; its per-cell state (Cell,
+ * cell.h:29-340: T_e, T_r, opacities, Fleck factor, energies) is read and
+ * written per field with bgs_get_cell_field / bgs_set_cell_field. */
 BGS_API int bgs_set_mesh(bgs_context *ctx, const bgs_mesh_desc *mesh);
 BGS_API uint32_t bgs_n_cells(const bgs_context *ctx);
 BGS_API int bgs_get_cell_field(bgs_context *ctx, int field, double *host_out);
 BGS_API int bgs_set_cell_field(bgs_context *ctx, int field, const double *host_in);
 
 /* ------------------------------------------------------- staged step */
+/* Each stage is one phase of imc_replicated_driver's step loop
+ * (replicated_driver.h:47-121), on the device. */
+/* Mesh::calculate_photon_energy (mesh.h:237-323): per-cell emission,
+ * boundary-source and (step 1) initial-census energies, their total, and the
+ * per-cell photon counts make_photons draws from them (source.h:207-366). */
 BGS_API int bgs_calculate_photon_energy(bgs_context *ctx, uint32_t step, double dt, bgs_energy_diag *out);
-/* Make this step's photons on the device after the census already in the
- * bank (step 1 also makes the initial census first). */
+/* make_photons (source.h:207-366, called at replicated_driver.h:73): this
+ * step's photons on the device after the census already in the bank (step 1
+ * also makes the initial census first). */
 BGS_API int bgs_source(bgs_context *ctx, uint32_t step, double dt);
-/* Transport every photon in the bank; census photons are compacted (in bank
- * order, life_dx = c*next_dt) into the other bank, which becomes current. */
+/* The transport of replicated_transport (replicated_transport.h:88-92:
+ * history_based_transport.h:279-343 in history mode, event_based_transport.h
+ * in event mode) and post_process_photons (post_process_functions.h:33-109):
+ * every photon in the bank; census photons are compacted (in bank order,
+ * life_dx = c*next_dt) into the other bank, which becomes current. */
 BGS_API int bgs_transport(bgs_context *ctx, double next_dt, uint32_t algorithm, bgs_transport_diag *out);
+/* The tally reduce (replicated_driver.h:90-94) and Mesh::update_temperature
+ * (mesh.h:327-423, called at replicated_driver.h:96). */
 BGS_API int bgs_update_temperature(bgs_context *ctx, double dt, bgs_transport_diag *out);
-/* All four stages; `out` may be NULL (then nothing is copied back and the
- * call does not wait for the GPU). */
+/* All four stages, one pass of the step loop (replicated_driver.h:47-121);
+ * `out` may be NULL (then nothing is copied back and the call does not wait
+ * for the GPU). */
 BGS_API int bgs_step(bgs_context *ctx, const bgs_step_params *p, bgs_transport_diag *out);
-/* Wait for the context's stream; returns BGS_ERR_DEVICE if a device check fired. */
+/* Wait for the context's stream; returns BGS_ERR_DEVICE if a device check
+ * fired.  No counterpart in the reference, whose calls return when done. */
 BGS_API int bgs_synchronize(bgs_context *ctx);
 
 /* --------------------------------------------------------- photon I/O */
+/* The driver's photon list (std::vector<Photon>, photon.h:33-183, or
+ * PhotonArray, photon_array.h:25-135), held on the device as the bank. */
 /* Number of photons in the current bank (the census after bgs_transport). */
 BGS_API int bgs_bank_size(bgs_context *ctx, uint64_t *n);
 /* Copy photons [offset, offset+count) of the current bank out / in. */
@@ -356,9 +375,11 @@ BGS_API int bgs_set_option(bgs_context *ctx, int option, double value);
 
 /* ------------------------------------------------------- instrumentation */
 /* Device time (ms) of the last transport kernel span, measured with CUDA
- * events on the context's stream, and its launch count. */
+ * events on the context's stream, and its launch count (the reference's
+ * transport timer, replicated_transport.h:63-143, times the same span). */
 BGS_API int bgs_last_transport_ms(bgs_context *ctx, float *ms, uint32_t *kernel_launches);
-/* Kernels launched by this context since creation (its own kernels only). */
+/* Kernels launched by this context since creation (its own kernels only).
+ * No counterpart in the reference. */
 BGS_API uint64_t bgs_kernel_launch_count(const bgs_context *ctx);
 
 #ifdef __cplusplus

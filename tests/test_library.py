@@ -64,3 +64,21 @@ def test_engine_fails_loudly_without_gpu():
     from branson_gb300._lib import BransonError
     with pytest.raises(BransonError):
         ReplicatedIMC(D.marshak_wave(photons=100))
+
+
+def test_every_entry_point_names_what_it_replaces():
+    """Each section of the C ABI header cites the upstream interface its entry
+    points replace (file:line), or says that the reference has no counterpart."""
+    lines = open(os.path.join(ROOT, "include", "branson_gb300.h")).read().splitlines()
+    missing = []
+    for i, line in enumerate(lines):
+        m = re.match(r"^BGS_API\s+[\w\s\*]+?\b(bgs_\w+)\s*\(", line)
+        if not m:
+            continue
+        j = i
+        while j > 0 and not lines[j].startswith("/* ----"):
+            j -= 1
+        section = "\n".join(lines[j:i + 1])
+        if not (re.search(r"\w+\.(h|in):\d+", section) or "counterpart" in section):
+            missing.append(m.group(1))
+    assert not missing, missing
