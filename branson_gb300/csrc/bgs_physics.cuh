@@ -235,12 +235,16 @@ __device__ __forceinline__ float rcp_approx(float x) {
 // by more than 2^-18 of their magnitudes, and every quotient from the 1e16
 // limit by more than 1e-4 of it, the exact comparisons order them the same
 // way and the division returns the distance the three-division form would.
+// A lane whose winner exceeds its collision distance by more than 2^-18
+// skips the division (the boundary is then not the event); FP64 work costs
+// the pipe per active lane, so the division runs on the pipe only for the
+// lanes whose boundary can come first.
 // Anything else (near ties, a zero or subnormal-range direction cosine, a
 // cosine image whose reciprocal flushes to zero, a quotient near 1e16 or
 // beyond float's range) returns false and the caller runs the three exact
 // divisions.
 __device__ __forceinline__ bool approx_faces(double ax, double ay, double az, const Lane &L, bool posx,
-                                             bool posy, bool posz, double &dist_to_boundary,
+                                             bool posy, bool posz, double dist_to_scatter, double &dist_to_boundary,
                                              long long &k_boundary, uint32_t &surface_cross) {
   float fax, fay, faz, fdx, fdy, fdz;
   bool ok = f32_image(ax, fax) & f32_image(ay, fay) & f32_image(az, faz);
@@ -273,12 +277,22 @@ __device__ __forceinline__ bool approx_faces(double ax, double ay, double az, co
     surface_cross = 0;
     return true;
   }
+  const bool pos = j == 0 ? posx : (j == 1 ? posy : posz);
+  surface_cross = 2u * (uint32_t)j + (pos ? 1u : 0u);
+  // the collision comes first by more than the quotients' error: the
+  // boundary is not the event and no comparison needs its exact distance
+  // (census first or collision first is then decided by those two alone),
+  // so that lane leaves the division out
+  float fs;
+  if (f32_image(dist_to_scatter, fs) && fs > 0.0f && m > fs * (1.0f + kTol)) {
+    dist_to_boundary = __longlong_as_double(0x7FF0000000000000LL);
+    k_boundary = 0x7FF0000000000000LL;
+    return true;
+  }
   const double a = j == 0 ? ax : (j == 1 ? ay : az);
   const double b = j == 0 ? L.dx : (j == 1 ? L.dy : L.dz);
-  const bool pos = j == 0 ? posx : (j == 1 ? posy : posz);
   dist_to_boundary = a / b;
   k_boundary = f64_key(dist_to_boundary);
-  surface_cross = 2u * (uint32_t)j + (pos ? 1u : 0u);
   return true;
 }
 
@@ -321,7 +335,7 @@ __device__ __forceinline__ int segment_advance(const MeshDev &m, const double *E
     ay = m.y[L.cj + (posy ? 1u : 0u)] - L.py;
     az = m.z[L.ck + (posz ? 1u : 0u)] - L.pz;
   }
-  if (!approx_faces(ax, ay, az, L, posx, posy, posz, dist_to_boundary, k_boundary, surface_cross)) {
+  if (!approx_faces(ax, ay, az, L, posx, posy, posz, dist_to_scatter, dist_to_boundary, k_boundary, surface_cross)) {
     double dist = ax / L.dx;
     long long k = f64_key(dist);
     if (k < k_boundary) { dist_to_boundary = dist; k_boundary = k; surface_cross = posx ? 1u : 0u; }
